@@ -1,0 +1,168 @@
+/* pars_gb300.h — C ABI of the GB300 (sm_103a) backend for the pars structural scan.
+ *
+ * Drop-in for the reference CUDA backend's public boundary
+ * (include/pars/backend/cuda/pipeline.cuh:722-1281, `pars::gpu::scanner<S>`):
+ * the grammar travels as the unchanged `pars::scan_plan` POD that
+ * `pars::compile::make_scan_plan<G>()` (include/pars/compile/plan.hpp:711-748)
+ * produces, passed by pointer and size instead of as a template argument, so one
+ * binary serves every grammar the DSL lowers.
+ *
+ * Conventions
+ *   - Every function returns 0 on success or a negative PARS_E* code; the library
+ *     never exits the process (the reference calls std::exit(1),
+ *     pipeline.cuh:520-555).  pars_last_error() gives a one-line reason.
+ *   - A pars_ctx owns one device, its scratch and output buffers; it is used by one
+ *     host thread at a time (like `scanner<S>`, whose methods are const with
+ *     mutable state).  Separate contexts may run concurrently.
+ *   - Device result pointers are borrowed from the context and stay valid until the
+ *     next scan call on the same context (pipeline.cuh:722-728).
+ *   - Streams are passed as `void*` holding a cudaStream_t (NULL = legacy stream).
+ *   - No torch or C++ types appear in this interface.
+ */
+#ifndef PARS_GB300_H
+#define PARS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes --------------------------------------------------------- */
+#define PARS_OK 0
+#define PARS_EINVAL (-22)   /* bad argument                                  */
+#define PARS_ENOMEM (-12)   /* device or pinned allocation failed            */
+#define PARS_EPLAN (-71)    /* malformed or unsupported scan_plan            */
+#define PARS_ECUDA (-5)     /* CUDA runtime error                            */
+#define PARS_ETIMEDOUT (-110) /* a bounded device wait gave up (error flag)  */
+#define PARS_ERANGE (-34)   /* input larger than 2^32-1 bytes (uint32 offsets) */
+#define PARS_EBUSY (-16)    /* arena full / request not admitted             */
+#define PARS_EAGAIN (-11)   /* request not finished yet                      */
+
+/* ---- the scan_plan POD --------------------------------------------------- */
+/* Byte-for-byte layout of pars::scan_plan (include/pars/plan.hpp:39-79): every
+ * member is a char/uint8_t/bool, so there is no padding; sizeof == 3177. */
+#define PARS_PLAN_BYTES 3177
+#define PARS_MAX_PUNCT 8
+#define PARS_MAX_BRACKETS 8
+#define PARS_MAX_MODES 8
+#define PARS_MAX_COMMENTS 4
+#define PARS_MAX_DFA_STATES 8
+#define PARS_MAX_DFA_CLASSES 8
+
+typedef struct pars_lex_desc {          /* scan_plan::lex_desc, plan.hpp:57-73 */
+  uint8_t kind;                         /* 0 affine 1 comment 2 doubled 3 table 4 fallback */
+  uint8_t n_states, n_classes, start;
+  uint8_t ok;
+  uint8_t delim, escape;
+  uint8_t rep_of[256];                  /* byte -> class */
+  uint8_t trans[PARS_MAX_DFA_STATES][PARS_MAX_DFA_CLASSES];   /* reset folded in */
+  uint8_t masked[PARS_MAX_DFA_STATES][PARS_MAX_DFA_CLASSES];
+} pars_lex_desc;
+
+typedef struct pars_scan_plan {         /* scan_plan, plan.hpp:39-79 */
+  uint8_t punctuation[PARS_MAX_PUNCT];
+  uint8_t brackets[PARS_MAX_BRACKETS][2];  /* {open, close} */
+  uint8_t modes[PARS_MAX_MODES][2];        /* {delim, escape} */
+  uint8_t comments[PARS_MAX_COMMENTS];
+  uint8_t n_punctuation, n_brackets, n_modes, n_comments;
+  pars_lex_desc descs[PARS_MAX_MODES];
+  uint8_t n_descs;
+} pars_scan_plan;
+
+/* ---- results -------------------------------------------------------------- */
+/* Flags for the scan calls. */
+#define PARS_WANT_PAIRS 1u    /* write pair_pos (structural space) and bracket_pair */
+#define PARS_RUN_PAIRS 2u     /* run R6: balanced / well_formed / max_depth          */
+#define PARS_WANT_CHARS 4u    /* write chars[] (structural byte values)              */
+#define PARS_WANT_MASK 8u     /* write the per-byte masked bitmap (needs 16-B aligned input) */
+#define PARS_FORCE_GENERIC 16u /* use the general descriptor kernel for every plan  */
+
+typedef struct pars_device_result {   /* cf. device_result, pipeline.cuh:722-728 */
+  const uint32_t* structural;    /* [n_struct] byte offsets of unmasked structural bytes */
+  const uint8_t* chars;          /* [n_struct] byte values, or NULL                     */
+  const int32_t* pair_pos;       /* [n_struct] partner's structural index, -1 if none   */
+  const uint32_t* bracket_pos;   /* [n_brackets] byte offsets of unmasked brackets      */
+  const uint8_t* bracket_char;   /* [n_brackets]                                         */
+  const uint32_t* bracket_struct;/* [n_brackets] structural index of each bracket       */
+  const int32_t* depth;          /* [n_brackets] depth key: open -> bal-1, close -> bal */
+  const int32_t* bracket_pair;   /* [n_brackets] partner's bracket index, -1 if none    */
+  const uint32_t* mask;          /* [ceil(n/32)] bit j of word w = byte 32w+j masked    */
+  uint64_t n_struct;
+  uint64_t n_brackets;
+  int32_t balanced;              /* nest.hpp:19-21 */
+  int32_t well_formed;
+  int32_t max_depth;
+  int32_t unclosed_mode;         /* scan.hpp:24,66-70 */
+  uint32_t kernel_path;          /* which scan kernel ran (diagnostic)                  */
+  uint32_t reserved;
+} pars_device_result;
+
+typedef struct pars_host_result {     /* cf. host_result, pipeline.cuh:730-735 */
+  const uint32_t* structural;    /* host pointers owned by the context (pinned)         */
+  const uint8_t* chars;
+  const int32_t* pair_pos;
+  uint64_t n_struct;
+  int32_t balanced, well_formed, max_depth, unclosed_mode;
+} pars_host_result;
+
+/* Carry between chunks of one document (cf. chunk_carry, pipeline.cuh:737-743).
+ * Opaque to the caller; zero-initialise it for the first chunk. */
+typedef struct pars_chunk_carry {
+  uint64_t state[4];
+  uint64_t out_base;       /* structural entries written so far */
+  uint64_t bracket_base;   /* bracket entries written so far    */
+  uint64_t byte_base;      /* bytes consumed so far             */
+} pars_chunk_carry;
+
+typedef struct pars_ctx pars_ctx;
+
+/* ---- context ------------------------------------------------------------- */
+/* Creates a context on `device`.  arena_bytes caps the device memory the context
+ * may hold (0 = grow on demand).  Replaces the per-thread scanner object and its
+ * DeviceCache (pipeline.cuh:562-714). */
+int pars_create(int device, uint64_t arena_bytes, pars_ctx** out);
+int pars_destroy(pars_ctx* ctx);
+const char* pars_last_error(const pars_ctx* ctx);
+/* ABI version and the plan POD size this build expects. */
+int pars_version(void);
+uint64_t pars_plan_bytes(void);
+
+/* ---- plans --------------------------------------------------------------- */
+/* Validates and uploads a scan_plan (the template argument S of scanner<S>). */
+int pars_plan_load(pars_ctx* ctx, const void* scan_plan, size_t len, int* plan_id);
+/* Which specialised scan path the plan maps to (diagnostic): 0 none, 1 parity,
+ * 2 doubled, 3 escape, 4 generic descriptor kernel. */
+int pars_plan_path(pars_ctx* ctx, int plan_id, int* path);
+
+/* ---- single document ----------------------------------------------------- */
+/* scanner<S>::scan_device (pipeline.cuh:1166-1173): device-resident input of n
+ * bytes (no padding required), results stay on the device.  Blocks until the
+ * result is ready.  n must be < 2^32. */
+int pars_scan_device(pars_ctx* ctx, int plan_id, const uint8_t* d_in, uint64_t n,
+                     uint32_t flags, void* stream, pars_device_result* out);
+
+/* scanner<S>::scan_host (pipeline.cuh:1176-1212): host input (pinned or pageable),
+ * results copied back to context-owned pinned host memory.  Large inputs are
+ * copied in chunks that overlap the scan. */
+int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n,
+                   uint32_t flags, void* stream, pars_host_result* out);
+
+/* scanner<S>::scan_chunk + reserve_struct + struct_ptr (pipeline.cuh:1214-1225):
+ * stage 1 (R1-R5) of one chunk of a longer document, for every plan kind.  The
+ * structural offsets of all chunks accumulate in the context's buffer, reported
+ * relative to the document start; the carry stays on the device between chunks
+ * (no host synchronisation per chunk).  pars_chunk_finish waits for the chunks
+ * issued so far, runs R6 over the whole document if requested, and fills `out`. */
+int pars_reserve_struct(pars_ctx* ctx, uint64_t cap);
+int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t n,
+                    pars_chunk_carry* carry, void* stream);
+int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
+                      uint32_t flags, void* stream, pars_device_result* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARS_GB300_H */

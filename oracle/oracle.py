@@ -1,0 +1,132 @@
+"""Python binding of the CPU oracle (oracle/pars_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and by
+``bench.py``'s CPU-baseline leg as the checker.  The product package
+``pars_gb300`` never imports it.
+
+The oracle restates the reference CPU backend: ``model::scanner<S>::scan``
+(include/pars/model/scan.hpp:33-72) and ``model::pair_brackets<S>``
+(include/pars/model/nest.hpp:46-92), with the plan passed at run time as the
+serialized ``scan_plan`` POD (include/pars/plan.hpp:39-79).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build() -> str:
+    """Compile liboracle.so with the committed Makefile (gcc only)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    return os.path.join(_HERE, "liboracle.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        src = os.path.join(_HERE, "pars_oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = ctypes.CDLL(path)
+        vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+        L.oracle_scan.restype = i32
+        L.oracle_scan.argtypes = [vp, u64, vp, u64, vp, vp, u64, vp, vp, u64, vp, vp]
+        L.oracle_pair.restype = i32
+        L.oracle_pair.argtypes = [vp, u64, vp, u64, vp, vp, vp]
+        L.oracle_time_scan_pair.restype = ctypes.c_double
+        L.oracle_time_scan_pair.argtypes = [vp, u64, vp, u64, i32, vp]
+        L.oracle_plan_bytes.restype = u64
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data if a.size else None
+
+
+@dataclass
+class ScanResult:
+    positions: np.ndarray  # uint32 structural byte offsets
+    chars: np.ndarray  # uint8
+    bracket_pos: np.ndarray  # uint32
+    bracket_char: np.ndarray  # uint8
+    mask: np.ndarray  # uint32 words, bit j of word w = masked(byte 32w+j)
+    unclosed_mode: bool
+
+
+@dataclass
+class PairResult:
+    pair: np.ndarray  # int32, bracket-index space, -1 when unpaired
+    depth: np.ndarray  # int32 depth key: open -> bal-1, close -> bal
+    balanced: bool
+    well_formed: bool
+    max_depth: int
+
+
+def scan(plan: bytes, data) -> ScanResult:
+    """R1-R5 exactly as scan.hpp:33-72 (plus the restated per-byte mask)."""
+    L = lib()
+    p = np.frombuffer(plan, np.uint8)
+    d = np.frombuffer(memoryview(data), np.uint8) if not isinstance(data, np.ndarray) else data
+    d = np.ascontiguousarray(d, dtype=np.uint8)
+    n = d.size
+    counts = np.zeros(3, np.uint64)
+    # first pass: counts only
+    rc = L.oracle_scan(p.ctypes.data, p.size, _ptr(d), n, None, None, 0, None, None, 0, None,
+                       counts.ctypes.data)
+    if rc != 0:
+        raise ValueError("malformed scan_plan")
+    ns, nb = int(counts[0]), int(counts[1])
+    pos = np.zeros(ns, np.uint32)
+    ch = np.zeros(ns, np.uint8)
+    bpos = np.zeros(nb, np.uint32)
+    bch = np.zeros(nb, np.uint8)
+    mask = np.zeros((n + 31) // 32, np.uint32)
+    L.oracle_scan(p.ctypes.data, p.size, _ptr(d), n, _ptr(pos), _ptr(ch), ns, _ptr(bpos),
+                  _ptr(bch), nb, _ptr(mask), counts.ctypes.data)
+    return ScanResult(pos, ch, bpos, bch, mask, bool(counts[2]))
+
+
+def pair(plan: bytes, bracket_char: np.ndarray) -> PairResult:
+    """R6 exactly as nest.hpp:46-92 (plus the restated depth keys)."""
+    L = lib()
+    p = np.frombuffer(plan, np.uint8)
+    b = np.ascontiguousarray(bracket_char, dtype=np.uint8)
+    n = b.size
+    pr = np.zeros(n, np.int32)
+    dep = np.zeros(n, np.int32)
+    fl = np.zeros(3, np.int32)
+    rc = L.oracle_pair(p.ctypes.data, p.size, _ptr(b), n, _ptr(pr), _ptr(dep), fl.ctypes.data)
+    if rc != 0:
+        raise ValueError("malformed scan_plan")
+    return PairResult(pr, dep, bool(fl[0]), bool(fl[1]), int(fl[2]))
+
+
+def pair_struct_space(sr: ScanResult, pr: PairResult) -> np.ndarray:
+    """Partner as a structural index (-1 for non-brackets / unpaired), the index
+    space of the reference GPU backend's pair_pos (pipeline.cuh:492-500)."""
+    out = np.full(sr.positions.size, -1, np.int32)
+    if sr.bracket_pos.size:
+        bsi = np.searchsorted(sr.positions, sr.bracket_pos).astype(np.int64)
+        partner = pr.pair
+        has = partner >= 0
+        out[bsi[has]] = bsi[partner[has]].astype(np.int32)
+    return out
+
+
+def time_scan_pair(plan: bytes, data: np.ndarray, iters: int = 1):
+    """Mean wall seconds per scan+pair on one host thread, and (n_struct, n_brackets)."""
+    L = lib()
+    p = np.frombuffer(plan, np.uint8)
+    d = np.ascontiguousarray(data, dtype=np.uint8)
+    counts = np.zeros(3, np.uint64)
+    s = L.oracle_time_scan_pair(p.ctypes.data, p.size, _ptr(d), d.size, iters, counts.ctypes.data)
+    return s, (int(counts[0]), int(counts[1]))

@@ -1,0 +1,139 @@
+// ref_driver.cpp — runs the UNMODIFIED reference CPU backend (pars model/scan.hpp and
+// model/nest.hpp, header-only) on files, to pin the oracle and make golden fixtures.
+//
+// TEST INFRASTRUCTURE ONLY.  Built by oracle/Makefile (target `ref`) against the
+// reference headers where they lie; the binary goes to oracle/_ref/ and is never
+// committed or shipped.  Where the reference has no output for a value (per-byte
+// masks, depth keys), this driver restates it next to the reference call from the
+// same plan object (scan.hpp:41-52; nest.hpp:55-76).
+//
+// Usage:
+//   ref_driver plans <outdir>                 write <grammar>.plan (raw scan_plan bytes)
+//   ref_driver run <grammar> <in> <outprefix> write <outprefix>.{pos,chars,bpos,bchar,
+//                                              pair,depth,mask,meta} for one input file
+#include "pars/pars.hpp"
+#include "grammars/json.hpp"
+#include "grammars/csv.hpp"
+#include "grammars/toml.hpp"
+#include "grammars/clike.hpp"
+#include "grammars/ini.hpp"
+#include "grammars/xml.hpp"
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+using namespace pars;
+
+static constexpr auto kJson	 = compile::make_scan_plan<bench::json_grammar>();
+static constexpr auto kCsv	 = compile::make_scan_plan<bench::csv_grammar>();
+static constexpr auto kToml	 = compile::make_scan_plan<bench::toml_grammar>();
+static constexpr auto kClike = compile::make_scan_plan<bench::clike_grammar>();
+static constexpr auto kIni	 = compile::make_scan_plan<bench::ini_grammar>();
+static constexpr auto kXml	 = compile::make_scan_plan<bench::xml_grammar>();
+
+template<class T>
+static void put(const std::string& path, const std::vector<T>& v) {
+	std::ofstream f(path, std::ios::binary);
+	f.write(reinterpret_cast<const char*>(v.data()), (std::streamsize)(v.size() * sizeof(T)));
+}
+
+static void put_plan(const std::string& dir, const char* name, const scan_plan& p) {
+	std::ofstream f(dir + "/" + name + ".plan", std::ios::binary);
+	f.write(reinterpret_cast<const char*>(&p), sizeof(scan_plan));
+}
+
+template<scan_plan S>
+static int run(const std::string& in_path, const std::string& out) {
+	std::ifstream	  f(in_path, std::ios::binary);
+	std::stringstream ss;
+	ss << f.rdbuf();
+	const std::string in = ss.str();
+
+	model::scanner<S> sc;
+	auto			  r = sc.scan(in);
+	auto			  t = model::pair_brackets<S>(r.bracket_char, r.bracket_pos);
+
+	// Restated values (not returned by the reference): per-byte mask (scan.hpp:41-52)
+	std::vector<std::uint32_t> mask((in.size() + 31) / 32, 0u);
+	{
+		std::array<std::uint8_t, kMaxModes> st {};
+		for (std::size_t d = 0; d < S.n_descs; ++d) st[d] = S.descs[d].start;
+		for (std::size_t i = 0; i < in.size(); ++i) {
+			const unsigned char c = static_cast<unsigned char>(in[i]);
+			bool				m = false;
+			for (std::size_t d = 0; d < S.n_descs; ++d) {
+				const auto& desc = S.descs[d];
+				const auto	cl	 = desc.rep_of[c];
+				if (desc.masked[st[d]][cl])
+					m = true;
+				st[d] = desc.trans[st[d]][cl];
+			}
+			if (m)
+				mask[i >> 5] |= 1u << (i & 31);
+		}
+	}
+	// ... and depth keys (nest.hpp:55-76).
+	std::vector<std::int32_t> depth(r.bracket_char.size());
+	{
+		int run = 0;
+		for (std::size_t i = 0; i < r.bracket_char.size(); ++i) {
+			const bool op = model::is_open_char(r.bracket_char[i], S);
+			run += op ? 1 : -1;
+			depth[i] = op ? run - 1 : run;
+		}
+	}
+	std::vector<std::uint8_t> bchar(r.bracket_char.begin(), r.bracket_char.end());
+	put(out + ".pos", r.positions);
+	put(out + ".chars", r.chars);
+	put(out + ".bpos", r.bracket_pos);
+	put(out + ".bchar", bchar);
+	put(out + ".pair", t.pair);
+	put(out + ".depth", depth);
+	put(out + ".mask", mask);
+	std::ofstream m(out + ".meta");
+	m << "n " << in.size() << "\n"
+	  << "n_struct " << r.positions.size() << "\n"
+	  << "n_brackets " << r.bracket_pos.size() << "\n"
+	  << "unclosed " << (r.unclosed_mode ? 1 : 0) << "\n"
+	  << "balanced " << (t.balanced ? 1 : 0) << "\n"
+	  << "well_formed " << (t.well_formed ? 1 : 0) << "\n"
+	  << "max_depth " << t.max_depth << "\n";
+	return 0;
+}
+
+int main(int argc, char** argv) {
+	if (argc >= 3 && std::strcmp(argv[1], "plans") == 0) {
+		const std::string dir = argv[2];
+		put_plan(dir, "json", kJson);
+		put_plan(dir, "csv", kCsv);
+		put_plan(dir, "toml", kToml);
+		put_plan(dir, "clike", kClike);
+		put_plan(dir, "ini", kIni);
+		put_plan(dir, "xml", kXml);
+		std::printf("sizeof(scan_plan)=%zu\n", sizeof(scan_plan));
+		return 0;
+	}
+	if (argc >= 5 && std::strcmp(argv[1], "run") == 0) {
+		const std::string g = argv[2];
+		if (g == "json")
+			return run<kJson>(argv[3], argv[4]);
+		if (g == "csv")
+			return run<kCsv>(argv[3], argv[4]);
+		if (g == "toml")
+			return run<kToml>(argv[3], argv[4]);
+		if (g == "clike")
+			return run<kClike>(argv[3], argv[4]);
+		if (g == "ini")
+			return run<kIni>(argv[3], argv[4]);
+		if (g == "xml")
+			return run<kXml>(argv[3], argv[4]);
+		std::fprintf(stderr, "unknown grammar %s\n", g.c_str());
+		return 2;
+	}
+	std::fprintf(stderr, "usage: ref_driver plans <dir> | run <grammar> <in> <outprefix>\n");
+	return 2;
+}

@@ -1,0 +1,13 @@
+"""pars_gb300 — GB300 (sm_103a) backend for the pars R1-R6 structural scan.
+
+The grammar arrives as the unchanged ``pars::scan_plan`` POD produced by the
+reference compiler (include/pars/compile/plan.hpp:711-748); the scan runs in
+hand-written CUDA behind the C ABI of include/pars_gb300.h.
+
+    from pars_gb300 import Scanner
+    sc = Scanner(open("json.plan", "rb").read())
+    r = sc.scan_tensor(data_u8_cuda, want_pairs=True)
+"""
+from .scanner import Context, DeviceResult, HostResult, Scanner  # noqa: F401
+
+__all__ = ["Context", "Scanner", "DeviceResult", "HostResult"]

@@ -1,0 +1,113 @@
+"""ctypes binding of the C ABI in include/pars_gb300.h (libpars_gb300.so).
+
+There is no fallback: importing this module on a machine without the built
+library raises, and every scan call goes to the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpars_gb300.so")
+
+PARS_WANT_PAIRS = 1
+PARS_RUN_PAIRS = 2
+PARS_WANT_CHARS = 4
+PARS_WANT_MASK = 8
+PARS_FORCE_GENERIC = 16
+
+ERRORS = {
+    -22: "PARS_EINVAL", -12: "PARS_ENOMEM", -71: "PARS_EPLAN", -5: "PARS_ECUDA",
+    -110: "PARS_ETIMEDOUT", -34: "PARS_ERANGE", -16: "PARS_EBUSY", -11: "PARS_EAGAIN",
+}
+
+PLAN_BYTES = 3177
+
+u8p = ctypes.POINTER(ctypes.c_uint8)
+u32p = ctypes.POINTER(ctypes.c_uint32)
+i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class DeviceResult(ctypes.Structure):
+    _fields_ = [
+        ("structural", ctypes.c_void_p), ("chars", ctypes.c_void_p),
+        ("pair_pos", ctypes.c_void_p), ("bracket_pos", ctypes.c_void_p),
+        ("bracket_char", ctypes.c_void_p), ("bracket_struct", ctypes.c_void_p),
+        ("depth", ctypes.c_void_p), ("bracket_pair", ctypes.c_void_p),
+        ("mask", ctypes.c_void_p),
+        ("n_struct", ctypes.c_uint64), ("n_brackets", ctypes.c_uint64),
+        ("balanced", ctypes.c_int32), ("well_formed", ctypes.c_int32),
+        ("max_depth", ctypes.c_int32), ("unclosed_mode", ctypes.c_int32),
+        ("kernel_path", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+    ]
+
+
+class HostResult(ctypes.Structure):
+    _fields_ = [
+        ("structural", ctypes.c_void_p), ("chars", ctypes.c_void_p),
+        ("pair_pos", ctypes.c_void_p), ("n_struct", ctypes.c_uint64),
+        ("balanced", ctypes.c_int32), ("well_formed", ctypes.c_int32),
+        ("max_depth", ctypes.c_int32), ("unclosed_mode", ctypes.c_int32),
+    ]
+
+
+class ChunkCarry(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_uint64 * 4), ("out_base", ctypes.c_uint64),
+                ("bracket_base", ctypes.c_uint64), ("byte_base", ctypes.c_uint64)]
+
+
+# Every function the header declares, with its ctypes signature.
+SIGNATURES = {
+    "pars_version": (ctypes.c_int, []),
+    "pars_plan_bytes": (ctypes.c_uint64, []),
+    "pars_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "pars_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    "pars_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pars_plan_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_int)]),
+    "pars_plan_path": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "pars_scan_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p,
+                                        ctypes.POINTER(DeviceResult)]),
+    "pars_scan_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p,
+                                      ctypes.POINTER(HostResult)]),
+    "pars_reserve_struct": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "pars_scan_chunk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_uint64, ctypes.POINTER(ChunkCarry),
+                                       ctypes.c_void_p]),
+    "pars_chunk_finish": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ChunkCarry),
+                                         ctypes.c_uint32, ctypes.c_void_p,
+                                         ctypes.POINTER(DeviceResult)]),
+}
+
+_LIB = None
+
+
+def lib():
+    """Load libpars_gb300.so and bind every declared entry point (raises if absent)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: the CUDA backend is not built "
+                              "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class ParsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def check(rc: int, ctx=None) -> None:
+    if rc != 0:
+        msg = lib().pars_last_error(ctx).decode() if ctx else ""
+        raise ParsError(rc, msg)

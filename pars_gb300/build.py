@@ -1,0 +1,87 @@
+"""In-tree build of the native parts (no cmake; a minute or two on a cold box).
+
+* ``pars_gb300/libpars_gb300.so`` — the CUDA backend (sm_103a only) and its C ABI
+  (include/pars_gb300.h);
+* ``pars_gb300/libpars_synth.so`` — seeded synthetic workload generators (host C++).
+
+Objects go to ``pars_gb300/_build/``.  Translation units compile in parallel.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+ROOT = os.path.dirname(HERE)
+
+CUDA_SOURCES = ["scan.cu", "pair.cu", "api.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-I", os.path.join(ROOT, "include")]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_cuda(verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(ROOT, "include", "pars_gb300.h"))
+    objs = []
+    jobs = []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
+    lib = os.path.join(HERE, "libpars_gb300.so")
+    if _stale(lib, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", lib, *objs])
+    if verbose:
+        print("built", lib)
+    return lib
+
+
+def build_synth() -> str:
+    lib = os.path.join(HERE, "libpars_synth.so")
+    src = os.path.join(CSRC, "synth.cpp")
+    if _stale(lib, [src]):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", lib, src])
+    return lib
+
+
+def build_all(verbose: bool = False) -> None:
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        f1 = ex.submit(build_cuda, verbose)
+        f2 = ex.submit(build_synth)
+        f1.result()
+        f2.result()
+
+
+if __name__ == "__main__":
+    build_all(verbose=True)

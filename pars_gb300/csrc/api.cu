@@ -1,0 +1,897 @@
+// api.cu — host driver and C ABI (include/pars_gb300.h).
+//
+// One pars_ctx per device/thread.  It owns grow-only device buffers (scratch and
+// outputs), a pinned result block, and the loaded plans.  A scan is:
+//   k_scan<path>            fused R1..R5 (scan.cu)
+//   k_sort_pass(first=1)    speculative single counting-sort pass of R6 (pair.cu)
+//   k_pair(require_ok=1)    adjacent pairing + flags
+//   D2H of the result block, one stream synchronisation
+// then host checks that may re-issue work: capacity overflow (grow, rerun), the
+// escape path's speculation guard (rerun on the generic kernel), and a key range
+// the single sort pass cannot take (LSD passes, then k_pair).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pars_gb300.h"
+#include "device.cuh"
+#include "pars_internal.h"
+
+namespace pars {
+
+// kernels (scan.cu / pair.cu)
+int		   scan_smem_bytes(int path);
+const void* scan_kernel(int path);
+int		   sort_tile_keys();
+struct SortPass;
+__global__ void k_sort_pass(const SortPass p);
+__global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, unsigned int shift,
+							 unsigned int* hist);
+__global__ void k_pair(const PairArgs a, int require_sort_ok);
+
+struct SortPass {
+	const std::int32_t*	 keys_in;
+	const std::uint32_t* idx_in;
+	std::int32_t*		 keys_out;
+	std::uint32_t*		 idx_out;
+	const std::uint32_t* digit_hist;
+	std::uint64_t*		 lb;
+	Counters*			 ctr;
+	DevResult*			 res;
+	const unsigned int*	 key_hist;
+	unsigned long long	 cap;
+	unsigned int		 shift;
+	unsigned int		 epoch;
+	int					 first;
+};
+
+}  // namespace pars
+
+using namespace pars;
+
+namespace {
+
+constexpr int kAbiVersion = 1;
+
+struct DevBuf {
+	void*  p	= nullptr;
+	size_t cap	= 0;
+};
+
+struct Plan {
+	pars_scan_plan raw;
+	DevPlan		   host;
+	DevPlan*	   dev = nullptr;
+	int			   path = kPathGeneric;
+};
+
+}  // namespace
+
+struct pars_ctx {
+	int				   device = 0;
+	uint64_t		   arena_limit = 0;	 // 0 = unlimited
+	uint64_t		   arena_used  = 0;
+	int				   num_sms	   = 0;
+	int				   scan_blocks[5] = {0, 0, 0, 0, 0};
+	std::string		   err;
+	std::vector<Plan*> plans;
+	unsigned int	   epoch = 0;
+
+	// scratch
+	DevBuf tiles, lb, sort_keys_a, sort_keys_b, sort_idx_b, digit_hist;
+	Counters*  ctr		= nullptr;
+	DevResult* res		= nullptr;
+	unsigned int* key_hist = nullptr;
+	DevCarry*  carry	= nullptr;	// [2] ping-pong for chunks
+	DevResult* h_res	= nullptr;	// pinned
+	// outputs
+	DevBuf pos, chars, pair, bpos, bchar, bsi, depth, bpair, order, mask;
+	uint64_t cap_s = 0, cap_b = 0;
+	// host-path staging
+	DevBuf		   d_in;
+	unsigned char* h_stage = nullptr;
+	size_t		   h_stage_cap = 0;
+	uint32_t*	   h_pos = nullptr;
+	uint8_t*	   h_chars = nullptr;
+	int32_t*	   h_pair = nullptr;
+	size_t		   h_out_cap = 0;
+	// chunk state
+	uint64_t chunk_index = 0;
+	cudaEvent_t ev = nullptr;
+};
+
+namespace {
+
+int fail(pars_ctx* c, int code, const char* fmt, const char* extra = "") {
+	if (c) {
+		char buf[512];
+		std::snprintf(buf, sizeof buf, fmt, extra);
+		c->err = buf;
+	}
+	return code;
+}
+
+int cuda_fail(pars_ctx* c, cudaError_t e, const char* what) {
+	if (c)
+		c->err = std::string(what) + ": " + cudaGetErrorString(e);
+	return e == cudaErrorMemoryAllocation ? PARS_ENOMEM : PARS_ECUDA;
+}
+
+#define CK(call)                                        \
+	do {                                                \
+		cudaError_t e_ = (call);                        \
+		if (e_ != cudaSuccess)                          \
+			return cuda_fail(ctx, e_, #call);           \
+	} while (0)
+
+int grow(pars_ctx* ctx, DevBuf& b, size_t bytes) {
+	if (bytes <= b.cap)
+		return 0;
+	size_t want = std::max(bytes, b.cap + b.cap / 2);
+	want		= (want + 4095) & ~size_t(4095);
+	if (ctx->arena_limit && ctx->arena_used - b.cap + want > ctx->arena_limit) {
+		want = bytes;
+		if (ctx->arena_used - b.cap + want > ctx->arena_limit)
+			return fail(ctx, PARS_ENOMEM, "arena limit reached");
+	}
+	if (b.p) {
+		cudaFree(b.p);
+		ctx->arena_used -= b.cap;
+		b.p	  = nullptr;
+		b.cap = 0;
+	}
+	cudaError_t e = cudaMalloc(&b.p, want);
+	if (e != cudaSuccess) {
+		cudaGetLastError();
+		return cuda_fail(ctx, e, "cudaMalloc");
+	}
+	b.cap = want;
+	ctx->arena_used += want;
+	return 0;
+}
+
+// ---- plan analysis -------------------------------------------------------------
+// Canonical automata of the fast paths, over byte roles X (other), Q (delimiter),
+// B (escape).  State 0 is the start.  entry = next | masked << 3; 0xFF = no role.
+struct Canon {
+	int			 n_states;
+	std::uint8_t t[4][3];
+};
+
+constexpr std::uint8_t M = 8;  // masked bit
+// parity: O0 -Q-> S -Q-> O2; S masks all it consumes
+constexpr Canon kParity {3, {{0, 1, 0xFF}, {1 | M, 2 | M, 0xFF}, {0, 1, 0xFF}, {0, 0, 0}}};
+// doubled: as parity, but O2 -Q-> S is masked
+constexpr Canon kDoubled {3, {{0, 1, 0xFF}, {1 | M, 2 | M, 0xFF}, {0, 1 | M, 0xFF}, {0, 0, 0}}};
+// escape: O0 -Q-> S, S -B-> E, E -any-> S, S -Q-> O2; backslash outside is inert
+constexpr Canon kEscape {4, {{0, 1, 0}, {1 | M, 2 | M, 3 | M}, {0, 1, 0}, {1 | M, 1 | M, 1 | M}}};
+
+// True when the descriptor, restricted to states reachable from its start, is
+// isomorphic (transitions, masked bits, and the start state) to `cn` under the
+// byte roles given by (delim, escape).
+bool isomorphic(const pars_lex_desc& d, const Canon& cn, int delim, int escape) {
+	auto role = [&](int c) { return c == delim ? 1 : (escape >= 0 && c == escape ? 2 : 0); };
+	int	 d2c[8], c2d[8];
+	for (int i = 0; i < 8; ++i) d2c[i] = c2d[i] = -1;
+	d2c[d.start] = 0;
+	c2d[0]		 = d.start;
+	int queue[8], qh = 0, qt = 0;
+	queue[qt++] = d.start;
+	while (qh < qt) {
+		const int ds = queue[qh++];
+		const int cs = d2c[ds];
+		for (int c = 0; c < 256; ++c) {
+			const int r	 = role(c);
+			const std::uint8_t ce = cn.t[cs][r];
+			if (ce == 0xFF)
+				return false;
+			const int cl = d.rep_of[c];
+			const int dn = d.trans[ds][cl];
+			const int dm = d.masked[ds][cl] ? 1 : 0;
+			const int cnx = ce & 7;
+			const int cm  = (ce & M) ? 1 : 0;
+			if (dm != cm)
+				return false;
+			if (d2c[dn] < 0 && c2d[cnx] < 0) {
+				d2c[dn]		= cnx;
+				c2d[cnx]	= dn;
+				queue[qt++] = dn;
+			} else if (d2c[dn] != cnx || c2d[cnx] != dn) {
+				return false;
+			}
+		}
+	}
+	return true;
+}
+
+int analyse_plan(const pars_scan_plan& p, DevPlan& h) {
+	std::memset(&h, 0, sizeof h);
+	if (p.n_punctuation > PARS_MAX_PUNCT || p.n_brackets > PARS_MAX_BRACKETS
+		|| p.n_modes > PARS_MAX_MODES || p.n_comments > PARS_MAX_COMMENTS
+		|| p.n_descs > PARS_MAX_MODES)
+		return -1;
+	for (int d = 0; d < p.n_descs; ++d) {
+		const pars_lex_desc& D = p.descs[d];
+		if (D.n_states == 0 || D.n_states > 8 || D.n_classes == 0 || D.n_classes > 8
+			|| D.start >= D.n_states)
+			return -1;
+		for (int c = 0; c < 256; ++c)
+			if (D.rep_of[c] >= D.n_classes)
+				return -1;
+		for (int s = 0; s < D.n_states; ++s)
+			for (int c = 0; c < D.n_classes; ++c)
+				if (D.trans[s][c] >= D.n_states)
+					return -1;
+	}
+	// R1 classifier (classify.hpp:39-55)
+	for (int i = 0; i < p.n_punctuation; ++i) h.cls[p.punctuation[i]] |= kClsStruct;
+	for (int i = 0; i < p.n_brackets; ++i) {
+		h.cls[p.brackets[i][0]] |= kClsStruct | kClsOpen;
+		h.cls[p.brackets[i][1]] |= kClsStruct | kClsClose;
+		h.is_open[p.brackets[i][0]]	 = 1;
+		h.is_close[p.brackets[i][1]] = 1;
+	}
+	// nest.hpp:40-44: the FIRST spec whose open byte matches decides the close byte
+	for (int i = p.n_brackets - 1; i >= 0; --i)
+		h.first_close[p.brackets[i][0]] = static_cast<std::uint16_t>(0x100u | p.brackets[i][1]);
+	h.has_brackets = p.n_brackets > 0 ? 1 : 0;
+	h.n_descs	   = p.n_descs;
+	for (int d = 0; d < p.n_descs; ++d) {
+		const pars_lex_desc& D = p.descs[d];
+		h.n_states[d]		   = D.n_states;
+		h.start[d]			   = D.start;
+		std::memcpy(h.rep_of[d], D.rep_of, 256);
+		for (int c = 0; c < 8; ++c) {
+			std::uint32_t lo = 0, hi = 0;
+			for (int s = 0; s < 8; ++s) {
+				const std::uint32_t nx = (s < D.n_states && c < D.n_classes) ? D.trans[s][c] : s;
+				if (s < 4)
+					lo |= nx << (8 * s);
+				else
+					hi |= nx << (8 * (s - 4));
+			}
+			h.tb_lo[d][c] = lo;
+			h.tb_hi[d][c] = hi;
+			for (int s = 0; s < 8; ++s) {
+				const int nx = (s < D.n_states && c < D.n_classes) ? D.trans[s][c] : s;
+				const int m	 = (s < D.n_states && c < D.n_classes && D.masked[s][c]) ? 1 : 0;
+				h.step[d][s][c] = static_cast<std::uint8_t>(nx | (m << 3));
+			}
+		}
+	}
+	int path = kPathGeneric;
+	if (p.n_descs == 0) {
+		path = kPathNone;
+	} else if (p.n_descs == 1) {
+		const pars_lex_desc& D = p.descs[0];
+		const int dl = D.delim, es = D.escape;
+		if (dl != 0 && es != 0 && es != dl && isomorphic(D, kEscape, dl, es))
+			path = kPathEscape;
+		else if (dl != 0 && isomorphic(D, kDoubled, dl, -1))
+			path = kPathDoubled;
+		else if (dl != 0 && isomorphic(D, kParity, dl, -1))
+			path = kPathParity;
+		if (path != kPathGeneric) {
+			h.delim		 = static_cast<std::uint8_t>(dl);
+			h.delim_rep	 = 0x01010101u * static_cast<std::uint32_t>(dl);
+			h.escape	 = static_cast<std::uint8_t>(es);
+			h.escape_rep = 0x01010101u * static_cast<std::uint32_t>(es);
+			h.cls[dl] |= kClsDelim;
+		}
+	}
+	h.path = path;
+	return path;
+}
+
+// ---- launch helpers --------------------------------------------------------------
+int ensure_scan_config(pars_ctx* ctx, int path) {
+	if (ctx->scan_blocks[path])
+		return 0;
+	const void* k	  = scan_kernel(path);
+	const int	smem = scan_smem_bytes(path);
+	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	int per_sm = 0;
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kScanThreads, smem));
+	if (per_sm < 1)
+		return fail(ctx, PARS_ECUDA, "scan kernel does not fit on an SM");
+	ctx->scan_blocks[path] = per_sm * ctx->num_sms;
+	return 0;
+}
+
+unsigned int next_epoch(pars_ctx* ctx) {
+	ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFu;
+	if (ctx->epoch == 0)
+		ctx->epoch = 1;
+	return ctx->epoch;
+}
+
+struct Scan {
+	const uint8_t* d_in;
+	uint64_t	   n;
+	uint32_t	   flags;
+	cudaStream_t   st;
+	int			   path;
+	const DevCarry* carry_in;
+	DevCarry*	   carry_out;
+};
+
+int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s) {
+	const uint64_t o	 = reinterpret_cast<uintptr_t>(s.d_in) & 15u;
+	const uint8_t* base	 = s.d_in - o;
+	const uint64_t total = o + s.n;
+	const uint64_t ntiles = (total + kTileBytes - 1) / kTileBytes;
+	const size_t tdesc = s.path == kPathGeneric ? sizeof(TileDescG) : sizeof(TileDesc);
+	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
+		return r;
+	if (int r = ensure_scan_config(ctx, s.path))
+		return r;
+	ScanArgs a {};
+	a.base		= base;
+	a.o			= o;
+	a.n			= s.n;
+	a.ntiles	= ntiles;
+	a.copy_end	= (total + 15) & ~uint64_t(15);
+	a.plan		= pl->dev;
+	a.pos		= static_cast<uint32_t*>(ctx->pos.p);
+	a.chars		= static_cast<uint8_t*>(ctx->chars.p);
+	a.pair		= static_cast<int32_t*>(ctx->pair.p);
+	a.cap_s		= ctx->cap_s;
+	a.bpos		= static_cast<uint32_t*>(ctx->bpos.p);
+	a.bchar		= static_cast<uint8_t*>(ctx->bchar.p);
+	a.bsi		= static_cast<uint32_t*>(ctx->bsi.p);
+	a.depth		= static_cast<int32_t*>(ctx->depth.p);
+	a.cap_b		= ctx->cap_b;
+	a.mask		= static_cast<uint32_t*>(ctx->mask.p);
+	a.tiles		= ctx->tiles.p;
+	a.ctr		= ctx->ctr;
+	a.res		= ctx->res;
+	a.key_hist	= ctx->key_hist;
+	a.carry_in	= s.carry_in;
+	a.carry_out = s.carry_out;
+	a.epoch		= next_epoch(ctx);
+	a.flags		= s.flags;
+	const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
+	void*	  args[] = {&a};
+	CK(cudaLaunchKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,
+						scan_smem_bytes(s.path), s.st));
+	return 0;
+}
+
+PairArgs pair_args(pars_ctx* ctx, const Plan* pl, uint32_t flags, const uint32_t* order) {
+	PairArgs p {};
+	p.depth	   = static_cast<const int32_t*>(ctx->depth.p);
+	p.bchar	   = static_cast<const uint8_t*>(ctx->bchar.p);
+	p.bsi	   = static_cast<const uint32_t*>(ctx->bsi.p);
+	p.order	   = const_cast<uint32_t*>(order);
+	p.pair	   = (flags & PARS_WANT_PAIRS) ? static_cast<int32_t*>(ctx->pair.p) : nullptr;
+	p.bpair	   = (flags & PARS_WANT_PAIRS) ? static_cast<int32_t*>(ctx->bpair.p) : nullptr;
+	p.ctr	   = ctx->ctr;
+	p.res	   = ctx->res;
+	p.key_hist = ctx->key_hist;
+	p.plan	   = pl->dev;
+	p.cap_b	   = ctx->cap_b;
+	p.cap_s	   = ctx->cap_s;
+	p.flags	   = flags;
+	return p;
+}
+
+int launch_pairs_speculative(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t st) {
+	const uint64_t ntiles_sort = (ctx->cap_b + sort_tile_keys() - 1) / sort_tile_keys() + 1;
+	if (int r = grow(ctx, ctx->lb, ntiles_sort * 256 * sizeof(uint64_t)))
+		return r;
+	SortPass sp {};
+	sp.keys_in	  = static_cast<const int32_t*>(ctx->depth.p);
+	sp.idx_out	  = static_cast<uint32_t*>(ctx->order.p);
+	sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
+	sp.ctr		  = ctx->ctr;
+	sp.res		  = ctx->res;
+	sp.key_hist	  = ctx->key_hist;
+	sp.cap		  = ctx->cap_b;
+	sp.epoch	  = next_epoch(ctx);
+	sp.first	  = 1;
+	const int grid = ctx->num_sms * 4;
+	void*	  a1[] = {&sp};
+	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(grid), dim3(256), a1, 0,
+						st));
+	PairArgs pa	  = pair_args(ctx, pl, flags, static_cast<const uint32_t*>(ctx->order.p));
+	int		 req  = 1;
+	void*	 a2[] = {&pa, &req};
+	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pair), dim3(ctx->num_sms * 4), dim3(256), a2,
+						0, st));
+	return 0;
+}
+
+// Host-driven LSD sort when the speculative single pass could not run.
+int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t st,
+				   const DevResult& r) {
+	const uint64_t n = r.n_brackets;
+	const uint64_t range = static_cast<uint64_t>(r.max_key - r.min_key) + 1;
+	int passes = 1;
+	while (passes < 4 && (range >> (8 * passes)) > 0) ++passes;
+	const uint64_t ntiles_sort = (n + sort_tile_keys() - 1) / sort_tile_keys() + 1;
+	if (int e = grow(ctx, ctx->lb, ntiles_sort * 256 * sizeof(uint64_t)))
+		return e;
+	if (int e = grow(ctx, ctx->sort_keys_a, n * 4 + 16))
+		return e;
+	if (int e = grow(ctx, ctx->sort_keys_b, n * 4 + 16))
+		return e;
+	if (int e = grow(ctx, ctx->sort_idx_b, n * 4 + 16))
+		return e;
+	if (int e = grow(ctx, ctx->digit_hist, 256 * 4))
+		return e;
+	const int32_t* kin	= static_cast<const int32_t*>(ctx->depth.p);
+	const uint32_t* iin = nullptr;
+	int32_t* kbuf[2]	= {static_cast<int32_t*>(ctx->sort_keys_a.p), static_cast<int32_t*>(ctx->sort_keys_b.p)};
+	uint32_t* ibuf[2]	= {static_cast<uint32_t*>(ctx->order.p), static_cast<uint32_t*>(ctx->sort_idx_b.p)};
+	// the last pass must land in ctx->order
+	int out = (passes % 2 == 1) ? 0 : 1;
+	for (int ps = 0; ps < passes; ++ps) {
+		CK(cudaMemsetAsync(ctx->digit_hist.p, 0, 256 * 4, st));
+		k_digit_hist<<<ctx->num_sms * 4, 256, 0, st>>>(kin, ctx->res, 8u * ps,
+													   static_cast<unsigned int*>(ctx->digit_hist.p));
+		CK(cudaGetLastError());
+		SortPass sp {};
+		sp.keys_in	  = kin;
+		sp.idx_in	  = iin;
+		sp.keys_out	  = (ps + 1 < passes) ? kbuf[out] : nullptr;
+		sp.idx_out	  = ibuf[out];
+		sp.digit_hist = static_cast<const uint32_t*>(ctx->digit_hist.p);
+		sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
+		sp.ctr		  = ctx->ctr;
+		sp.res		  = ctx->res;
+		sp.key_hist	  = ctx->key_hist;
+		sp.cap		  = n;
+		sp.shift	  = 8u * ps;
+		sp.epoch	  = next_epoch(ctx);
+		sp.first	  = 0;
+		void* a1[]	  = {&sp};
+		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4),
+							dim3(256), a1, 0, st));
+		kin = kbuf[out];
+		iin = ibuf[out];
+		out ^= 1;
+	}
+	PairArgs pa	  = pair_args(ctx, pl, flags, static_cast<const uint32_t*>(ctx->order.p));
+	int		 req  = 0;
+	void*	 a2[] = {&pa, &req};
+	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pair), dim3(ctx->num_sms * 4), dim3(256), a2,
+						0, st));
+	return 0;
+}
+
+int ensure_outputs(pars_ctx* ctx, uint64_t cap_s, uint64_t cap_b, uint64_t n, uint32_t flags) {
+	cap_s = std::max<uint64_t>(cap_s, 1024);
+	cap_b = std::max<uint64_t>(cap_b, 1024);
+	if (int r = grow(ctx, ctx->pos, cap_s * 4))
+		return r;
+	if ((flags & PARS_WANT_CHARS))
+		if (int r = grow(ctx, ctx->chars, cap_s))
+			return r;
+	if ((flags & PARS_WANT_PAIRS))
+		if (int r = grow(ctx, ctx->pair, cap_s * 4))
+			return r;
+	if (int r = grow(ctx, ctx->bpos, cap_b * 4))
+		return r;
+	if (int r = grow(ctx, ctx->bchar, cap_b))
+		return r;
+	if (int r = grow(ctx, ctx->bsi, cap_b * 4))
+		return r;
+	if (int r = grow(ctx, ctx->depth, cap_b * 4))
+		return r;
+	if (int r = grow(ctx, ctx->order, cap_b * 4))
+		return r;
+	if ((flags & PARS_WANT_PAIRS))
+		if (int r = grow(ctx, ctx->bpair, cap_b * 4))
+			return r;
+	if ((flags & PARS_WANT_MASK))
+		if (int r = grow(ctx, ctx->mask, ((n + 31) / 32) * 4 + 64))
+			return r;
+	// capacities actually usable by this call
+	ctx->cap_s = ctx->pos.cap / 4;
+	if ((flags & PARS_WANT_CHARS))
+		ctx->cap_s = std::min<uint64_t>(ctx->cap_s, ctx->chars.cap);
+	if ((flags & PARS_WANT_PAIRS))
+		ctx->cap_s = std::min<uint64_t>(ctx->cap_s, ctx->pair.cap / 4);
+	ctx->cap_b = std::min<uint64_t>({ctx->bpos.cap / 4, ctx->bchar.cap, ctx->bsi.cap / 4,
+									 ctx->depth.cap / 4, ctx->order.cap / 4});
+	if ((flags & PARS_WANT_PAIRS))
+		ctx->cap_b = std::min<uint64_t>(ctx->cap_b, ctx->bpair.cap / 4);
+	return 0;
+}
+
+int reset_after_error(pars_ctx* ctx, cudaStream_t st) {
+	CK(cudaStreamSynchronize(st));
+	CK(cudaMemset(ctx->ctr, 0, sizeof(Counters)));
+	CK(cudaMemset(ctx->res, 0, sizeof(DevResult)));
+	if (ctx->tiles.p)
+		CK(cudaMemset(ctx->tiles.p, 0, ctx->tiles.cap));
+	if (ctx->lb.p)
+		CK(cudaMemset(ctx->lb.p, 0, ctx->lb.cap));
+	return 0;
+}
+
+void fill_result(pars_ctx* ctx, const DevResult& r, uint32_t flags, bool pairs_ran,
+				 pars_device_result* out) {
+	std::memset(out, 0, sizeof *out);
+	out->structural	  = static_cast<const uint32_t*>(ctx->pos.p);
+	out->chars		  = (flags & PARS_WANT_CHARS) ? static_cast<const uint8_t*>(ctx->chars.p) : nullptr;
+	out->pair_pos	  = (flags & PARS_WANT_PAIRS) && pairs_ran ? static_cast<const int32_t*>(ctx->pair.p) : nullptr;
+	out->bracket_pos  = static_cast<const uint32_t*>(ctx->bpos.p);
+	out->bracket_char = static_cast<const uint8_t*>(ctx->bchar.p);
+	out->bracket_struct = static_cast<const uint32_t*>(ctx->bsi.p);
+	out->depth		  = static_cast<const int32_t*>(ctx->depth.p);
+	out->bracket_pair = (flags & PARS_WANT_PAIRS) && pairs_ran ? static_cast<const int32_t*>(ctx->bpair.p) : nullptr;
+	out->mask		  = (flags & PARS_WANT_MASK) ? static_cast<const uint32_t*>(ctx->mask.p) : nullptr;
+	out->n_struct	  = r.n_struct;
+	out->n_brackets	  = r.n_brackets;
+	out->unclosed_mode = r.unclosed ? 1 : 0;
+	if (pairs_ran) {
+		out->balanced	 = r.balanced ? 1 : 0;
+		out->well_formed = r.well_formed ? 1 : 0;
+		out->max_depth	 = r.max_depth;
+	} else {
+		out->balanced	 = 1;
+		out->well_formed = 1;
+		out->max_depth	 = 0;
+	}
+	out->kernel_path = r.path;
+}
+
+Plan* get_plan(pars_ctx* ctx, int id) {
+	if (!ctx || id < 0 || id >= static_cast<int>(ctx->plans.size()))
+		return nullptr;
+	return ctx->plans[id];
+}
+
+// The whole single-document pipeline on a device buffer (blocking).
+int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, uint32_t flags,
+					 cudaStream_t st, pars_device_result* out) {
+	if (n >= (1ull << 32))
+		return fail(ctx, PARS_ERANGE, "document larger than 2^32-1 bytes");
+	if (n > 0 && !d_in)
+		return fail(ctx, PARS_EINVAL, "null input");
+	if ((flags & PARS_WANT_MASK) && (reinterpret_cast<uintptr_t>(d_in) & 15u))
+		return fail(ctx, PARS_EINVAL, "PARS_WANT_MASK needs a 16-byte aligned input");
+	const bool run_pairs = (flags & PARS_RUN_PAIRS) && pl->host.has_brackets;
+	if (n == 0) {
+		DevResult z {};
+		z.balanced = z.well_formed = 1;
+		fill_result(ctx, z, flags, run_pairs, out);
+		out->kernel_path = pl->path;
+		return 0;
+	}
+	int path = (flags & PARS_FORCE_GENERIC) ? kPathGeneric : pl->path;
+	uint64_t want_s = std::max<uint64_t>(ctx->cap_s, n / 3 + 4096);
+	uint64_t want_b = std::max<uint64_t>(ctx->cap_b, pl->host.has_brackets ? n / 6 + 4096 : 1024);
+	for (int attempt = 0; attempt < 4; ++attempt) {
+		if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
+			return r;
+		Scan s {d_in, n, flags, st, path, nullptr, nullptr};
+		if (int r = launch_scan(ctx, pl, s))
+			return r;
+		if (run_pairs)
+			if (int r = launch_pairs_speculative(ctx, pl, flags, st))
+				return r;
+		CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		DevResult r = *ctx->h_res;
+		if (r.error) {
+			reset_after_error(ctx, st);
+			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+		}
+		if (r.n_struct > ctx->cap_s || r.n_brackets > ctx->cap_b) {
+			want_s = std::max<uint64_t>(want_s, r.n_struct + 1024);
+			want_b = std::max<uint64_t>(want_b, r.n_brackets + 1024);
+			continue;
+		}
+		if (path == kPathEscape && r.spec_fail) {
+			path = kPathGeneric;  // exact descriptor semantics for this input
+			continue;
+		}
+		if (run_pairs && !r.sort_ok) {
+			if (int e = pairs_fallback(ctx, pl, flags, st, r))
+				return e;
+			CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+			CK(cudaStreamSynchronize(st));
+			r = *ctx->h_res;
+			if (r.error) {
+				reset_after_error(ctx, st);
+				return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+			}
+		}
+		fill_result(ctx, r, flags, run_pairs, out);
+		return 0;
+	}
+	return fail(ctx, PARS_ECUDA, "scan did not converge");
+}
+
+}  // namespace
+
+// ================================================================================
+// C ABI
+// ================================================================================
+extern "C" {
+
+int pars_version(void) {
+	return kAbiVersion;
+}
+
+uint64_t pars_plan_bytes(void) {
+	return sizeof(pars_scan_plan);
+}
+
+const char* pars_last_error(const pars_ctx* ctx) {
+	return ctx ? ctx->err.c_str() : "null context";
+}
+
+int pars_create(int device, uint64_t arena_bytes, pars_ctx** out) {
+	static_assert(sizeof(pars_scan_plan) == PARS_PLAN_BYTES, "scan_plan layout");
+	if (!out)
+		return PARS_EINVAL;
+	*out		  = nullptr;
+	pars_ctx* ctx = new pars_ctx();
+	ctx->device	  = device;
+	ctx->arena_limit = arena_bytes;
+	cudaError_t e = cudaSetDevice(device);
+	if (e != cudaSuccess) {
+		delete ctx;
+		return PARS_ECUDA;
+	}
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	ctx->num_sms = sms > 0 ? sms : 1;
+	auto bail = [&](cudaError_t err) {
+		pars_destroy(ctx);
+		return err == cudaErrorMemoryAllocation ? PARS_ENOMEM : PARS_ECUDA;
+	};
+	if ((e = cudaMalloc(&ctx->ctr, sizeof(Counters))) != cudaSuccess) return bail(e);
+	if ((e = cudaMalloc(&ctx->res, sizeof(DevResult))) != cudaSuccess) return bail(e);
+	if ((e = cudaMalloc(&ctx->key_hist, 2 * kKeyWindow * sizeof(unsigned int))) != cudaSuccess) return bail(e);
+	if ((e = cudaMalloc(&ctx->carry, 2 * sizeof(DevCarry))) != cudaSuccess) return bail(e);
+	if ((e = cudaMemset(ctx->ctr, 0, sizeof(Counters))) != cudaSuccess) return bail(e);
+	if ((e = cudaMemset(ctx->res, 0, sizeof(DevResult))) != cudaSuccess) return bail(e);
+	if ((e = cudaMemset(ctx->carry, 0, 2 * sizeof(DevCarry))) != cudaSuccess) return bail(e);
+	if ((e = cudaHostAlloc(&ctx->h_res, sizeof(DevResult), cudaHostAllocDefault)) != cudaSuccess)
+		return bail(e);
+	if ((e = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+	*out = ctx;
+	return 0;
+}
+
+int pars_destroy(pars_ctx* ctx) {
+	if (!ctx)
+		return PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	cudaDeviceSynchronize();
+	for (DevBuf* b : {&ctx->tiles, &ctx->lb, &ctx->sort_keys_a, &ctx->sort_keys_b, &ctx->sort_idx_b,
+					  &ctx->digit_hist, &ctx->pos, &ctx->chars, &ctx->pair, &ctx->bpos, &ctx->bchar,
+					  &ctx->bsi, &ctx->depth, &ctx->bpair, &ctx->order, &ctx->mask, &ctx->d_in})
+		if (b->p)
+			cudaFree(b->p);
+	if (ctx->ctr) cudaFree(ctx->ctr);
+	if (ctx->res) cudaFree(ctx->res);
+	if (ctx->key_hist) cudaFree(ctx->key_hist);
+	if (ctx->carry) cudaFree(ctx->carry);
+	if (ctx->h_res) cudaFreeHost(ctx->h_res);
+	if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+	if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
+	if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
+	if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
+	if (ctx->ev) cudaEventDestroy(ctx->ev);
+	for (Plan* p : ctx->plans) {
+		if (p->dev)
+			cudaFree(p->dev);
+		delete p;
+	}
+	delete ctx;
+	return 0;
+}
+
+int pars_plan_load(pars_ctx* ctx, const void* scan_plan, size_t len, int* plan_id) {
+	if (!ctx || !scan_plan || !plan_id)
+		return PARS_EINVAL;
+	if (len != sizeof(pars_scan_plan))
+		return fail(ctx, PARS_EPLAN, "scan_plan must be %s bytes", "3177");
+	Plan* pl = new Plan();
+	std::memcpy(&pl->raw, scan_plan, sizeof(pars_scan_plan));
+	if (analyse_plan(pl->raw, pl->host) < 0) {
+		delete pl;
+		return fail(ctx, PARS_EPLAN, "malformed scan_plan");
+	}
+	pl->path = pl->host.path;
+	cudaSetDevice(ctx->device);
+	cudaError_t e = cudaMalloc(&pl->dev, sizeof(DevPlan));
+	if (e == cudaSuccess)
+		e = cudaMemcpy(pl->dev, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		if (pl->dev)
+			cudaFree(pl->dev);
+		delete pl;
+		return cuda_fail(ctx, e, "plan upload");
+	}
+	ctx->plans.push_back(pl);
+	*plan_id = static_cast<int>(ctx->plans.size()) - 1;
+	return 0;
+}
+
+int pars_plan_path(pars_ctx* ctx, int plan_id, int* path) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !path)
+		return PARS_EINVAL;
+	*path = pl->path;
+	return 0;
+}
+
+int pars_scan_device(pars_ctx* ctx, int plan_id, const uint8_t* d_in, uint64_t n, uint32_t flags,
+					 void* stream, pars_device_result* out) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !out)
+		return ctx ? fail(ctx, PARS_EINVAL, "bad plan id or null result") : PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	return scan_device_impl(ctx, pl, d_in, n, flags, static_cast<cudaStream_t>(stream), out);
+}
+
+int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, uint32_t flags,
+				   void* stream, pars_host_result* out) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !out || (n && !h_in))
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	if (int r = grow(ctx, ctx->d_in, n + 16))
+		return r;
+	// pinned input goes straight to the device; pageable input through a pinned stage
+	cudaPointerAttributes attr {};
+	const bool pinned = cudaPointerGetAttributes(&attr, h_in) == cudaSuccess
+					 && (attr.type == cudaMemoryTypeHost);
+	cudaGetLastError();
+	if (n) {
+		if (pinned) {
+			CK(cudaMemcpyAsync(ctx->d_in.p, h_in, n, cudaMemcpyHostToDevice, st));
+		} else {
+			const size_t chunk = 64u << 20;
+			if (ctx->h_stage_cap < chunk) {
+				if (ctx->h_stage)
+					cudaFreeHost(ctx->h_stage);
+				CK(cudaHostAlloc(&ctx->h_stage, chunk, cudaHostAllocDefault));
+				ctx->h_stage_cap = chunk;
+			}
+			for (uint64_t off = 0; off < n; off += chunk) {
+				const size_t len = static_cast<size_t>(std::min<uint64_t>(chunk, n - off));
+				CK(cudaStreamSynchronize(st));
+				std::memcpy(ctx->h_stage, h_in + off, len);
+				CK(cudaMemcpyAsync(static_cast<uint8_t*>(ctx->d_in.p) + off, ctx->h_stage, len,
+								   cudaMemcpyHostToDevice, st));
+			}
+		}
+	}
+	pars_device_result dr {};
+	if (int r = scan_device_impl(ctx, pl, static_cast<const uint8_t*>(ctx->d_in.p), n, flags, st, &dr))
+		return r;
+	const size_t need = dr.n_struct;
+	if (need > ctx->h_out_cap) {
+		if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
+		if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
+		if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
+		ctx->h_pos = nullptr;
+		ctx->h_chars = nullptr;
+		ctx->h_pair = nullptr;
+		const size_t cap = need + need / 2 + 1024;
+		CK(cudaHostAlloc(&ctx->h_pos, cap * 4, cudaHostAllocDefault));
+		CK(cudaHostAlloc(&ctx->h_chars, cap, cudaHostAllocDefault));
+		CK(cudaHostAlloc(&ctx->h_pair, cap * 4, cudaHostAllocDefault));
+		ctx->h_out_cap = cap;
+	}
+	if (need) {
+		CK(cudaMemcpyAsync(ctx->h_pos, dr.structural, need * 4, cudaMemcpyDeviceToHost, st));
+		if (dr.chars)
+			CK(cudaMemcpyAsync(ctx->h_chars, dr.chars, need, cudaMemcpyDeviceToHost, st));
+		if (dr.pair_pos)
+			CK(cudaMemcpyAsync(ctx->h_pair, dr.pair_pos, need * 4, cudaMemcpyDeviceToHost, st));
+	}
+	CK(cudaStreamSynchronize(st));
+	out->structural	   = ctx->h_pos;
+	out->chars		   = dr.chars ? ctx->h_chars : nullptr;
+	out->pair_pos	   = dr.pair_pos ? ctx->h_pair : nullptr;
+	out->n_struct	   = dr.n_struct;
+	out->balanced	   = dr.balanced;
+	out->well_formed   = dr.well_formed;
+	out->max_depth	   = dr.max_depth;
+	out->unclosed_mode = dr.unclosed_mode;
+	return 0;
+}
+
+int pars_reserve_struct(pars_ctx* ctx, uint64_t cap) {
+	if (!ctx)
+		return PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	return ensure_outputs(ctx, cap, std::max<uint64_t>(ctx->cap_b, cap), 0,
+						  PARS_WANT_PAIRS | PARS_WANT_CHARS);
+}
+
+int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t n,
+					pars_chunk_carry* carry, void* stream) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !carry || (n && !d_chunk))
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	if (carry->byte_base + n >= (1ull << 32))
+		return fail(ctx, PARS_ERANGE, "document larger than 2^32-1 bytes");
+	cudaSetDevice(ctx->device);
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	if (carry->byte_base == 0) {
+		// first chunk of a document: fresh carry, fresh chunk index
+		ctx->chunk_index = 0;
+		DevCarry z {};
+		for (int d = 0; d < 8; ++d) z.gstate[d] = d < pl->host.n_descs ? pl->host.start[d] : 0;
+		CK(cudaMemcpyAsync(ctx->carry, &z, sizeof z, cudaMemcpyHostToDevice, st));
+		if (ctx->cap_s == 0)
+			if (int r = ensure_outputs(ctx, 1 << 20, 1 << 20, 0, PARS_WANT_PAIRS | PARS_WANT_CHARS))
+				return r;
+	}
+	if (n == 0)
+		return 0;
+	const int path = pl->path == kPathEscape ? kPathGeneric : pl->path;
+	DevCarry* cin  = ctx->carry + (ctx->chunk_index & 1);
+	DevCarry* cout = ctx->carry + ((ctx->chunk_index + 1) & 1);
+	Scan s {d_chunk, n, PARS_WANT_PAIRS | PARS_WANT_CHARS, st, path, cin, cout};
+	if (int r = launch_scan(ctx, pl, s))
+		return r;
+	ctx->chunk_index++;
+	carry->byte_base += n;
+	carry->state[0] = ctx->chunk_index;
+	return 0;
+}
+
+int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry, uint32_t flags,
+					  void* stream, pars_device_result* out) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !carry || !out)
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	const bool run_pairs = (flags & PARS_RUN_PAIRS) && pl->host.has_brackets;
+	if (carry->byte_base == 0) {
+		DevResult z {};
+		z.balanced = z.well_formed = 1;
+		fill_result(ctx, z, flags, run_pairs, out);
+		return 0;
+	}
+	// the last chunk's last tile left cumulative counts, the running depth extrema
+	// and the key histogram of the whole document in the result block
+	CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	DevResult r = *ctx->h_res;
+	if (r.error) {
+		reset_after_error(ctx, st);
+		return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+	}
+	if (r.n_struct > ctx->cap_s || r.n_brackets > ctx->cap_b)
+		return fail(ctx, PARS_ENOMEM, "chunk outputs exceeded the reserved capacity");
+	if (run_pairs) {
+		if (int e = launch_pairs_speculative(ctx, pl, flags | PARS_WANT_PAIRS, st))
+			return e;
+		CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		r = *ctx->h_res;
+		if (!r.sort_ok && !r.error) {
+			if (int e = pairs_fallback(ctx, pl, flags | PARS_WANT_PAIRS, st, r))
+				return e;
+			CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+			CK(cudaStreamSynchronize(st));
+			r = *ctx->h_res;
+		}
+		if (r.error) {
+			reset_after_error(ctx, st);
+			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+		}
+	}
+	fill_result(ctx, r, flags, run_pairs, out);
+	return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,164 @@
+// device.cuh — shared device-side definitions of the pars GB300 backend.
+//
+// Layout of the scratch the kernels share (all owned by a pars_ctx):
+//   TileDesc[]   per 16 KiB input tile: two decoupled-lookback chains
+//                (chain 1: the R4 automaton element; chain 2: R5 counts)
+//   DevResult    one per scan: counts, depth extrema, flags
+//   Counters     dynamic tile tickets and CTA-exit counters (self-resetting)
+//   key_hist     2048-bin histogram of bracket depth keys in [-1024, 1024)
+#pragma once
+
+#include <cstdint>
+
+#include "pars_internal.h"
+
+namespace pars {
+
+constexpr int kScanThreads = 512;           // one 32-byte word per thread
+constexpr int kTileBytes   = kScanThreads * 32;  // 16 KiB per tile
+constexpr int kStages      = 3;             // TMA bulk-copy pipeline depth
+constexpr int kKeyWindow   = 1024;          // key histogram covers [-1024, 1024)
+
+// Status word of a lookback chain: (epoch << 2) | flag.
+constexpr std::uint32_t kFlagAgg  = 1;
+constexpr std::uint32_t kFlagIncl = 2;
+
+// Bounded spin: after this many polls (with nanosleep back-off) a wait gives up,
+// records PARS_DEV_ERR_TIMEOUT in DevResult::error and unwinds.
+constexpr std::uint32_t kSpinLimit = 1u << 22;
+
+struct __align__(64) TileDesc {
+	std::uint32_t st1, st2;		   // chain status words
+	std::uint32_t agg1, inc1;	   // chain 1 element (fast paths)
+	std::uint64_t agg2[3];		   // chain 2: n_struct, n_open, n_close of this tile
+	std::uint64_t inc2[3];		   // chain 2 inclusive prefix
+};
+
+struct __align__(64) TileDescG {   // generic path: one nibble-packed map per descriptor
+	std::uint32_t st1, st2;
+	std::uint32_t agg1[8];
+	std::uint32_t inc1[8];
+	std::uint32_t pad[2];
+	std::uint64_t agg2[3];
+	std::uint64_t inc2[3];
+};
+
+struct Counters {
+	unsigned int scan_ticket, scan_done;
+	unsigned int sort_ticket, sort_done;
+	unsigned int pair_done;
+	unsigned int pad[11];
+};
+
+// ---- PTX helpers --------------------------------------------------------------
+__device__ __forceinline__ std::uint32_t smem_addr(const void* p) {
+	return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void st_release(std::uint32_t* p, std::uint32_t v) {
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ std::uint32_t ld_acquire(const std::uint32_t* p) {
+	std::uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ std::uint32_t ld_relaxed(const std::uint32_t* p) {
+	std::uint32_t v;
+	asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ std::uint64_t ld_relaxed64(const std::uint64_t* p) {
+	std::uint64_t v;
+	asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_relaxed64(std::uint64_t* p, std::uint64_t v) {
+	asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void st_release64(std::uint64_t* p, std::uint64_t v) {
+	asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ std::uint64_t ld_acquire64(const std::uint64_t* p) {
+	std::uint64_t v;
+	asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void mbar_init(std::uint64_t* bar, std::uint32_t count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+				 : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(std::uint64_t* bar, std::uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+				 "r"(bytes)
+				 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, std::uint32_t phase) {
+	std::uint32_t ok;
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t}"
+		: "=r"(ok)
+		: "r"(smem_addr(bar)), "r"(phase)
+		: "memory");
+	return ok != 0;
+}
+
+// 1-D TMA: global -> shared, completion counted on `bar`.  `bytes` must be a
+// multiple of 16 and both addresses 16-byte aligned.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, std::uint32_t bytes,
+										 std::uint64_t* bar) {
+	asm volatile(
+		"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+			"r"(smem_addr(dst)),
+		"l"(src), "r"(bytes), "r"(smem_addr(bar))
+		: "memory");
+}
+
+__device__ __forceinline__ std::uint32_t prmt(std::uint32_t a, std::uint32_t b, std::uint32_t s) {
+	return __byte_perm(a, b, s);
+}
+
+// Inclusive prefix-xor of the bits of a 32-bit word (bit j = xor of bits 0..j).
+__device__ __forceinline__ std::uint32_t prefix_xor32(std::uint32_t x) {
+	x ^= x << 1;
+	x ^= x << 2;
+	x ^= x << 4;
+	x ^= x << 8;
+	x ^= x << 16;
+	return x;
+}
+
+// Bits [lo, hi) set, for 0 <= lo <= hi <= 32.
+__device__ __forceinline__ std::uint32_t bit_range(int lo, int hi) {
+	const std::uint32_t up = hi >= 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u);
+	const std::uint32_t dn = lo >= 32 ? 0xFFFFFFFFu : ((1u << lo) - 1u);
+	return up & ~dn;
+}
+
+// Device-side error codes recorded in DevResult::error.
+constexpr std::uint32_t kDevErrTimeout = 1;
+
+__device__ __forceinline__ bool aborted(const DevResult* r) {
+	return ld_relaxed(&r->error) != 0;
+}
+
+__device__ __forceinline__ void record_error(DevResult* r, std::uint32_t code) {
+	atomicOr(&r->error, code);
+}
+
+}  // namespace pars

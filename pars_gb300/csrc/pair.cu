@@ -1,0 +1,309 @@
+// pair.cu — R6 bracket pairing on the GPU.
+//
+// Reference semantics (include/pars/model/nest.hpp:46-92): bal = inclusive +-1
+// prefix over the bracket sequence; key = open ? bal-1 : bal; stable sort of
+// bracket indices by key; pair order[2k] with order[2k+1] when the first is an
+// open bracket, the second a close bracket, and the first bracket spec opening
+// with that byte closes with that byte; balanced = min(bal) >= 0 && bal[n-1] == 0;
+// well_formed = every pair typed + even count + balanced; max_depth = max(0, bal).
+//
+// The scan kernel already produced the keys (depth[]), their extrema and a
+// 2048-bin histogram over [-1024, 1024), so R6 here is:
+//   k_sort_pass  one stable counting-sort pass (onesweep: per-tile ranks with
+//                warp match-any, per-bucket decoupled look-back across tiles) on an
+//                8-bit digit of key - min_key, writing (optionally) keys and the
+//                bracket index;
+//   k_digit_hist the digit histogram for passes the scan's window cannot provide;
+//   k_pair       adjacent pairing + type check, then the last CTA folds the flags.
+// The common case (key range <= 256, all keys in the window) is ONE sort pass
+// launched without a host round-trip; anything else is finished by the host with
+// LSD passes over 8-bit digits.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace pars {
+
+namespace {
+
+constexpr unsigned kFull		  = 0xFFFFFFFFu;
+constexpr int	   kSortThreads	  = 256;
+constexpr int	   kSortItems	  = 16;
+constexpr int	   kSortTile	  = kSortThreads * kSortItems;	// 4096 keys
+constexpr int	   kSortWarps	  = kSortThreads / 32;
+
+// Look-back word of one (tile, bucket): flag(2) | epoch(22) | count(40).
+__device__ __forceinline__ std::uint64_t pack_lb(std::uint32_t flag, std::uint32_t epoch,
+												 std::uint64_t cnt) {
+	return (static_cast<std::uint64_t>(flag) << 62)
+		 | (static_cast<std::uint64_t>(epoch & 0x3FFFFFu) << 40) | (cnt & 0xFFFFFFFFFFull);
+}
+
+}  // namespace
+
+struct SortPass {
+	const std::int32_t*	 keys_in;	 // [n]
+	const std::uint32_t* idx_in;	 // [n] or null (identity)
+	std::int32_t*		 keys_out;	 // [n] or null
+	std::uint32_t*		 idx_out;	 // [n]
+	const std::uint32_t* digit_hist; // [256] or null: take it from the key window
+	std::uint64_t*		 lb;		 // look-back words [tiles][256]
+	Counters*			 ctr;
+	DevResult*			 res;
+	const unsigned int*	 key_hist;	 // [2048] window histogram
+	unsigned long long	 cap;		 // capacity of the key / index buffers
+	unsigned int		 shift;
+	unsigned int		 epoch;
+	int					 first;		 // 1: the speculative single pass (checks the range)
+};
+
+// One stable counting-sort pass over digit = ((key - min_key) >> shift) & 255.
+__global__ void __launch_bounds__(kSortThreads) k_sort_pass(const SortPass p) {
+	__shared__ unsigned int whist[kSortWarps][256];
+	__shared__ unsigned int gbase[256];
+	__shared__ unsigned int texcl[256];
+	__shared__ unsigned long long s_tile;
+	__shared__ int			s_fail;
+
+	DevResult* res = p.res;
+	const int  tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const unsigned long long n = res->n_brackets;
+	const long long			 kmin = res->min_key;
+
+	if (p.first) {
+		// speculative single pass: only when every key sits in the window and the
+		// key range fits one 8-bit digit
+		const bool ok = !res->keys_oob && !res->error && n <= p.cap
+					 && (n == 0 || res->max_key - kmin < 256);
+		if (blockIdx.x == 0 && tid == 0)
+			res->sort_ok = ok ? 1u : 0u;
+		if (!ok || n == 0)
+			return;
+	}
+	// global base of each digit bucket
+	{
+		unsigned int c = 0;
+		if (p.digit_hist) {
+			c = p.digit_hist[tid];
+		} else {
+			const long long k = kmin + tid;
+			if (k >= -kKeyWindow && k < kKeyWindow)
+				c = p.key_hist[k + kKeyWindow];
+		}
+		// block exclusive scan of 256 counts
+		unsigned int x = c;
+#pragma unroll
+		for (int off = 1; off < 32; off <<= 1) {
+			const unsigned int y = __shfl_up_sync(kFull, x, off);
+			if (lane >= off)
+				x += y;
+		}
+		if (lane == 31)
+			whist[0][warp] = x;
+		__syncthreads();
+		unsigned int wpre = 0;
+		for (int w = 0; w < warp; ++w) wpre += whist[0][w];
+		gbase[tid] = wpre + x - c;
+		__syncthreads();
+	}
+	const std::uint32_t epoch = p.epoch & 0x3FFFFFu;
+	const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
+	if (tid == 0)
+		s_fail = 0;
+	while (true) {
+		if (tid == 0)
+			s_tile = atomicAdd(&p.ctr->sort_ticket, 1u);
+		for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
+		__syncthreads();
+		const unsigned long long t = s_tile;
+		if (t >= ntiles || s_fail)
+			break;
+		// ---- rank: warp w owns 512 consecutive keys, 16 rounds of 32 ----------------
+		const unsigned long long wbase = t * kSortTile + static_cast<unsigned long long>(warp) * 512;
+		std::uint32_t			 dig[kSortItems];
+		std::uint32_t			 rnk[kSortItems];
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			std::uint32_t			 d = 0xFFFFFFFFu;
+			if (e < n)
+				d = static_cast<std::uint32_t>(
+						static_cast<unsigned long long>(p.keys_in[e] - kmin) >> p.shift)
+				  & 255u;
+			const std::uint32_t peers = __match_any_sync(kFull, d);
+			const std::uint32_t below = peers & ((1u << lane) - 1u);
+			std::uint32_t		base  = 0;
+			if (d != 0xFFFFFFFFu)
+				base = whist[warp][d];
+			__syncwarp();
+			if (d != 0xFFFFFFFFu && below == 0)
+				whist[warp][d] = base + __popc(peers);
+			__syncwarp();
+			dig[i] = d;
+			rnk[i] = base + __popc(below);
+		}
+		__syncthreads();
+		// ---- per-bucket tile total and warp offsets ----------------------------------
+		unsigned int tot = 0;
+		for (int w = 0; w < kSortWarps; ++w) {
+			const unsigned int c = whist[w][tid];
+			whist[w][tid]		 = tot;	 // becomes the warp's exclusive offset
+			tot += c;
+		}
+		// ---- per-bucket decoupled look-back ------------------------------------------
+		std::uint64_t* row = p.lb + t * 256;
+		unsigned long long excl = 0;
+		if (t == 0) {
+			st_release64(&row[tid], pack_lb(kFlagIncl, epoch, tot));
+		} else {
+			st_release64(&row[tid], pack_lb(kFlagAgg, epoch, tot));
+			long long j	   = static_cast<long long>(t) - 1;
+			std::uint32_t spins = 0;
+			while (j >= 0) {
+				const std::uint64_t w = ld_acquire64(p.lb + j * 256 + tid);
+				const std::uint32_t f = static_cast<std::uint32_t>(w >> 62);
+				const std::uint32_t e = static_cast<std::uint32_t>(w >> 40) & 0x3FFFFFu;
+				if (e != epoch || f == 0) {
+					if (++spins > kSpinLimit) {
+						record_error(res, kDevErrTimeout);
+						s_fail = 1;
+						break;
+					}
+					if ((spins & 63u) == 0 && aborted(res)) {
+						s_fail = 1;
+						break;
+					}
+					__nanosleep(64);
+					continue;
+				}
+				excl += w & 0xFFFFFFFFFFull;
+				if (f == kFlagIncl)
+					break;
+				--j;
+			}
+			st_release64(&row[tid], pack_lb(kFlagIncl, epoch, excl + tot));
+		}
+		texcl[tid] = static_cast<unsigned int>(excl);
+		__syncthreads();
+		// ---- scatter ----------------------------------------------------------------
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			const std::uint32_t		 d = dig[i];
+			if (d == 0xFFFFFFFFu)
+				continue;
+			const unsigned long long dst =
+				static_cast<unsigned long long>(gbase[d]) + texcl[d] + whist[warp][d] + rnk[i];
+			p.idx_out[dst] = p.idx_in ? p.idx_in[e] : static_cast<std::uint32_t>(e);
+			if (p.keys_out)
+				p.keys_out[dst] = p.keys_in[e];
+		}
+		__syncthreads();
+	}
+	__syncthreads();
+	if (tid == 0) {
+		__threadfence();
+		const unsigned int done = atomicAdd(&p.ctr->sort_done, 1u);
+		if (done == gridDim.x - 1) {
+			p.ctr->sort_ticket = 0;
+			p.ctr->sort_done   = 0;
+			__threadfence();
+		}
+	}
+}
+
+// Histogram of one 8-bit digit of key - min_key (host-driven LSD passes).
+__global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, unsigned int shift,
+							 unsigned int* hist) {
+	__shared__ unsigned int h[256];
+	h[threadIdx.x] = 0;
+	__syncthreads();
+	const unsigned long long n	  = res->n_brackets;
+	const long long			 kmin = res->min_key;
+	for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += gridDim.x * 256ull) {
+		const std::uint32_t d =
+			static_cast<std::uint32_t>(static_cast<unsigned long long>(keys[i] - kmin) >> shift)
+			& 255u;
+		atomicAdd(&h[d], 1u);
+	}
+	__syncthreads();
+	if (h[threadIdx.x])
+		atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// Adjacent pairing over the sorted order, then flags (last CTA).
+__global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort_ok) {
+	__shared__ std::uint8_t	 s_open[256], s_close[256];
+	__shared__ std::uint16_t s_first[256];
+	__shared__ unsigned int	 s_bad;
+	DevResult* res = a.res;
+	const int  tid = threadIdx.x;
+	if (require_sort_ok && !res->sort_ok)
+		return;
+	s_open[tid]	 = a.plan->is_open[tid];
+	s_close[tid] = a.plan->is_close[tid];
+	s_first[tid] = a.plan->first_close[tid];
+	if (tid == 0)
+		s_bad = 0;
+	__syncthreads();
+	const unsigned long long n		 = res->n_brackets;
+	if (n > a.cap_b || res->n_struct > a.cap_s)
+		return;	 // outputs overflowed: the host grows the buffers and reruns
+	const unsigned long long npairs = (n + 1) / 2;
+	const bool want = (a.flags & 1u) != 0;
+	unsigned int bad = 0;
+	for (unsigned long long r = blockIdx.x * 256ull + tid; r < npairs; r += gridDim.x * 256ull) {
+		const std::uint32_t ia = a.order[2 * r];
+		if (2 * r + 1 >= n) {  // odd count: the last entry has no partner
+			if (want) {
+				if (a.bpair)
+					a.bpair[ia] = -1;
+				if (a.pair)
+					a.pair[a.bsi[ia]] = -1;
+			}
+			continue;
+		}
+		const std::uint32_t ib = a.order[2 * r + 1];
+		const std::uint8_t	ca = a.bchar[ia], cb = a.bchar[ib];
+		const bool ok = s_open[ca] && s_close[cb] && s_first[ca] == (0x100u | cb);
+		if (!ok)
+			bad = 1;
+		if (want) {
+			if (a.bpair) {
+				a.bpair[ia] = ok ? static_cast<std::int32_t>(ib) : -1;
+				a.bpair[ib] = ok ? static_cast<std::int32_t>(ia) : -1;
+			}
+			if (a.pair) {
+				const std::uint32_t sa = a.bsi[ia], sb = a.bsi[ib];
+				a.pair[sa] = ok ? static_cast<std::int32_t>(sb) : -1;
+				a.pair[sb] = ok ? static_cast<std::int32_t>(sa) : -1;
+			}
+		}
+	}
+	if (__any_sync(kFull, bad) && (tid & 31) == 0)
+		atomicOr(&s_bad, 1u);
+	__syncthreads();
+	if (tid == 0) {
+		if (s_bad)
+			atomicOr(&res->mismatch, 1u);
+		__threadfence();
+		const unsigned int done = atomicAdd(&a.ctr->pair_done, 1u);
+		if (done == gridDim.x - 1) {
+			__threadfence();
+			const long long	 fin = static_cast<long long>(res->n_open) - static_cast<long long>(res->n_close);
+			const bool		 bal = res->min_bal >= 0 && fin == 0;
+			const unsigned int mis = *reinterpret_cast<volatile unsigned int*>(&res->mismatch);
+			res->balanced		 = bal ? 1u : 0u;
+			res->well_formed	 = (bal && !mis && (n % 2 == 0)) ? 1u : 0u;
+			res->max_depth		 = static_cast<int>(res->max_bal > 0 ? res->max_bal : 0);
+			a.ctr->pair_done	 = 0;
+			__threadfence();
+		}
+	}
+}
+
+int sort_tile_keys() {
+	return kSortTile;
+}
+
+}  // namespace pars

@@ -1,0 +1,134 @@
+// pars_internal.h — structures shared by the host driver and the CUDA kernels.
+// Not part of the public C ABI (include/pars_gb300.h).
+#pragma once
+
+#include <cstdint>
+
+namespace pars {
+
+// Scan-kernel paths.  A plan maps to one of them when it is loaded:
+//   kPathNone    — no lexical descriptor: nothing is masked.
+//   kPathParity  — one descriptor isomorphic to the no-escape quote automaton
+//                  (XML attribute / TOML literal string shape):
+//                  O -q-> S -q-> O2, S masks every byte it consumes.
+//   kPathDoubled — one descriptor isomorphic to the doubled-delimiter automaton
+//                  (CSV "" shape): like parity, but a quote right after a closing
+//                  quote is masked (it re-opens the field).
+//   kPathEscape  — one descriptor isomorphic to the prefix-escape automaton
+//                  (JSON string shape): a backslash inside a string masks itself
+//                  and the next byte.
+//   kPathGeneric — anything else: every descriptor runs as a packed state map.
+enum : int { kPathNone = 0, kPathParity = 1, kPathDoubled = 2, kPathEscape = 3, kPathGeneric = 4 };
+
+// Classifier bits of DevPlan::cls (one flag per byte lane of a 32-bit word, so
+// that 8 consecutive lookups can be summed into one register without carries).
+constexpr std::uint32_t kClsStruct = 1u << 0;
+constexpr std::uint32_t kClsOpen   = 1u << 8;
+constexpr std::uint32_t kClsClose  = 1u << 16;
+constexpr std::uint32_t kClsDelim  = 1u << 24;
+
+struct DevPlan {
+	std::uint32_t cls[256];			   // R1 classifier (classify.hpp:39-55) + fast-path delim
+	std::uint8_t  is_open[256];		   // nest.hpp:24-30
+	std::uint8_t  is_close[256];	   // nest.hpp:32-38
+	std::uint16_t first_close[256];	   // nest.hpp:40-44: 0x100 | close of first spec opening c
+	// generic descriptor tables
+	std::uint8_t  rep_of[8][256];	   // byte -> class per descriptor
+	std::uint32_t tb_lo[8][8];		   // [desc][class]: next state of states 0..3, one per byte
+	std::uint32_t tb_hi[8][8];		   // [desc][class]: next state of states 4..7
+	std::uint8_t  step[8][8][8];	   // [desc][state][class]: next | masked << 3
+	std::uint8_t  n_states[8];
+	std::uint8_t  start[8];
+	std::int32_t  n_descs;
+	std::int32_t  path;
+	std::uint32_t delim_rep;		   // fast paths: delimiter byte replicated x4
+	std::uint32_t escape_rep;		   // escape path: escape byte replicated x4
+	std::uint8_t  delim;
+	std::uint8_t  escape;
+	std::uint8_t  has_brackets;
+	std::uint8_t  pad0;
+};
+
+// Per-scan result block written by the kernels and read back by the host.
+struct DevResult {
+	unsigned long long n_struct;
+	unsigned long long n_brackets;
+	unsigned long long n_open;
+	unsigned long long n_close;
+	long long		   min_bal;	   // min over brackets of the running depth (init 0)
+	long long		   max_bal;	   // max over brackets of the running depth (init 0)
+	long long		   min_key;
+	long long		   max_key;
+	unsigned int	   unclosed;
+	unsigned int	   spec_fail;	// escape path: a quote escaped outside a string
+	unsigned int	   keys_oob;	// a depth key fell outside [-1024, 1024)
+	unsigned int	   error;		// bounded wait gave up (kDevErrTimeout)
+	unsigned int	   sort_ok;
+	unsigned int	   mismatch;
+	unsigned int	   balanced;
+	unsigned int	   well_formed;
+	int				   max_depth;
+	unsigned int	   path;
+	unsigned int	   pad[2];
+};
+
+// State at a chunk boundary (device resident; chained chunk to chunk).
+struct DevCarry {
+	unsigned int	   fstate;		// fast paths: bit0 escape pending, bit1 in-string parity
+	unsigned int	   last_delim;	// previous byte was the delimiter (doubled path)
+	unsigned int	   last_toggle; // previous byte toggled the string state
+	unsigned int	   unclosed;
+	unsigned int	   gstate[8];	// generic path: state of each descriptor
+	unsigned long long ns, no, nc;	// structural / open / close counts so far
+	unsigned long long byte_base;	// bytes consumed so far
+	unsigned long long pad;
+};
+
+struct Counters;
+
+struct ScanArgs {
+	const std::uint8_t*	 base;		// input rounded down to 16 bytes
+	unsigned long long	 o;			// base + o = first document byte
+	unsigned long long	 n;			// document bytes
+	unsigned long long	 ntiles;	// ceil((o + n) / 16 KiB)
+	unsigned long long	 copy_end;	// bytes of [base, base + copy_end) that may be read
+	const DevPlan*		 plan;
+	std::uint32_t*		 pos;
+	std::uint8_t*		 chars;
+	std::int32_t*		 pair;
+	unsigned long long	 cap_s;
+	std::uint32_t*		 bpos;
+	std::uint8_t*		 bchar;
+	std::uint32_t*		 bsi;
+	std::int32_t*		 depth;
+	unsigned long long	 cap_b;
+	std::uint32_t*		 mask;
+	void*				 tiles;
+	Counters*			 ctr;
+	DevResult*			 res;
+	unsigned int*		 key_hist;
+	const DevCarry*		 carry_in;	// null for a whole document
+	DevCarry*			 carry_out; // null for a whole document
+	unsigned int		 epoch;
+	unsigned int		 flags;
+};
+
+struct PairArgs {
+	const std::int32_t*	 depth;		// [n_brackets] keys
+	const std::uint8_t*	 bchar;
+	const std::uint32_t* bsi;
+	std::uint32_t*		 order;		// [n_brackets] bracket indices sorted by (key, index)
+	std::int32_t*		 pair;		// structural space, may be null
+	std::int32_t*		 bpair;		// bracket space, may be null
+	std::uint64_t*		 sort_tiles;
+	Counters*			 ctr;
+	DevResult*			 res;
+	const unsigned int*	 key_hist;
+	const DevPlan*		 plan;
+	unsigned long long	 cap_b;
+	unsigned long long	 cap_s;
+	unsigned int		 epoch;
+	unsigned int		 flags;
+};
+
+}  // namespace pars

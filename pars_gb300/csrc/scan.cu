@@ -1,0 +1,995 @@
+// scan.cu — fused R1..R5 single-pass structural scan for one GB300 (sm_103a).
+//
+// One persistent kernel streams the document through shared memory in 16 KiB
+// tiles (1-D TMA bulk copies, 3-stage mbarrier pipeline) and, per tile:
+//   R1  classifies every byte against a per-lane replicated 256-entry table in
+//       shared memory (conflict-free: lane l reads column l), summing 8 lookups
+//       into one register per 8 bytes and transposing the four flag planes with
+//       byte permutes into 32-bit masks (structural, open, close, delimiter);
+//   R4  forms the automaton element of its 32-byte word (an affine map on the
+//       2-bit state (escape pending, in-string parity) for the fast paths, or a
+//       nibble-packed state map per descriptor for the generic path), scans it
+//       across the block with warp shuffles and across tiles with a decoupled
+//       look-back (chain 1);
+//   R2/R3 turns the resolved state into the per-byte masked bitmap and selects
+//       structural / open / close bits outside it;
+//   R5  counts them (chain 2 look-back gives each tile its output offsets) and
+//       writes uint32 offsets, bracket arrays and the bracket depth keys, which
+//       feed R6 (pair.cu) without another pass over the input.
+//
+// Reference semantics: include/pars/model/scan.hpp:33-72 (per-byte descriptor
+// loop, masked bytes skipped, structural bytes and brackets appended in order,
+// unclosed_mode when any descriptor ends off its start state) and
+// include/pars/model/nest.hpp:55-76 (bal = inclusive +-1 prefix, key = open ?
+// bal-1 : bal).  The reference GPU backend does the same work as ~12 launches
+// with host syncs (include/pars/backend/cuda/pipeline.cuh:753-1017).
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace pars {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// ---- fast-path automaton element -------------------------------------------
+// State: bit0 e = "next byte is escaped", bit1 p = "inside a string".
+// Element (a, b, q, d) maps (e, p) -> (a&e ^ b, p ^ q ^ d&e); bits a=0 b=1 q=2 d=3.
+constexpr std::uint32_t kIdent = 1u;
+
+__device__ __forceinline__ std::uint32_t compose_fast(std::uint32_t X, std::uint32_t Y) {
+	const std::uint32_t aX = X & 1u, bX = (X >> 1) & 1u, qX = (X >> 2) & 1u, dX = (X >> 3) & 1u;
+	const std::uint32_t aY = Y & 1u, bY = (Y >> 1) & 1u, qY = (Y >> 2) & 1u, dY = (Y >> 3) & 1u;
+	return (aX & aY) | (((bX & aY) ^ bY) << 1) | ((qX ^ qY ^ (bX & dY)) << 2)
+		 | ((dX ^ (aX & dY)) << 3);
+}
+
+__device__ __forceinline__ std::uint32_t apply_fast(std::uint32_t X, std::uint32_t s) {
+	const std::uint32_t e = s & 1u, p = (s >> 1) & 1u;
+	const std::uint32_t a = X & 1u, b = (X >> 1) & 1u, q = (X >> 2) & 1u, d = (X >> 3) & 1u;
+	return ((a & e) ^ b) | ((p ^ q ^ (d & e)) << 1);
+}
+
+// ---- generic-path element: one nibble-packed map per descriptor --------------
+struct Maps {
+	std::uint32_t m[8];
+};
+
+constexpr std::uint32_t kIdentMap = 0x76543210u;
+
+// nibble map -> byte tables (states 0..3 in lo, 4..7 in hi)
+__device__ __forceinline__ void nib_to_bytes(std::uint32_t m, std::uint32_t& lo, std::uint32_t& hi) {
+	const std::uint32_t x = m & 0x0F0F0F0Fu;		 // nibbles 0,2,4,6 at byte lanes
+	const std::uint32_t y = (m >> 4) & 0x0F0F0F0Fu;	 // nibbles 1,3,5,7
+	lo					  = prmt(x, y, 0x5140);		 // states 0,1,2,3
+	hi					  = prmt(x, y, 0x7362);		 // states 4,5,6,7
+}
+
+// byte lanes (values < 16) of two words -> 8 nibbles
+__device__ __forceinline__ std::uint32_t bytes_to_nib(std::uint32_t lo, std::uint32_t hi) {
+	const std::uint32_t a = (lo | (lo >> 4)) & 0x00FF00FFu;
+	const std::uint32_t b = (hi | (hi >> 4)) & 0x00FF00FFu;
+	return prmt(a, b, 0x6420);
+}
+
+// (Y o X): apply X first.  X nibble map; Y as byte tables (lo, hi).
+__device__ __forceinline__ std::uint32_t then_map(std::uint32_t X, std::uint32_t Ylo,
+												  std::uint32_t Yhi) {
+	const std::uint32_t r0 = prmt(Ylo, Yhi, X & 0xFFFFu);
+	const std::uint32_t r1 = prmt(Ylo, Yhi, X >> 16);
+	return bytes_to_nib(r0, r1);
+}
+
+__device__ __forceinline__ std::uint32_t compose_map(std::uint32_t X, std::uint32_t Y) {
+	std::uint32_t lo, hi;
+	nib_to_bytes(Y, lo, hi);
+	return then_map(X, lo, hi);
+}
+
+// ---- shared scratch -----------------------------------------------------------
+struct Scratch {
+	unsigned long long tile_id[kStages];
+	std::uint32_t	   warp_elem[16];
+	std::uint32_t	   warp_maps[16][8];
+	std::uint32_t	   warp_cnt[16][3];
+	std::uint32_t	   tile_excl_elem;
+	std::uint32_t	   tile_excl_maps[8];
+	std::uint32_t	   init_state;
+	std::uint32_t	   init_gstate[8];
+	unsigned long long base_cnt[3];
+	long long		   wmin_bal[16], wmax_bal[16], wmin_key[16], wmax_key[16];
+	std::uint32_t	   any_br;
+	std::uint32_t	   failed;
+};
+
+constexpr int kTableBytes = 256 * 32 * 4;
+
+// ---- bounded look-back --------------------------------------------------------
+// Waits until tile `idx`'s status carries this launch's epoch and a flag.
+// Returns the status word, or 0 when the wait gave up (error recorded).
+__device__ __forceinline__ std::uint32_t wait_status(const std::uint32_t* st, std::uint32_t epoch,
+													 DevResult* res) {
+	std::uint32_t spins = 0;
+	while (true) {
+		const std::uint32_t s = ld_acquire(st);
+		if ((s >> 2) == epoch && (s & 3u))
+			return s;
+		if (++spins > kSpinLimit) {
+			record_error(res, kDevErrTimeout);
+			return 0;
+		}
+		if ((spins & 63u) == 0 && aborted(res))
+			return 0;
+		__nanosleep(spins < 64 ? 32 : 256);
+	}
+}
+
+// Chain 1 (fast element): exclusive prefix of tiles [0, t).  Executed by one warp.
+__device__ std::uint32_t lookback_fast(TileDesc* tiles, unsigned long long t, std::uint32_t epoch,
+									   DevResult* res, int lane, bool& fail) {
+	std::uint32_t excl = kIdent;
+	long long	  j	   = static_cast<long long>(t) - 1;
+	while (j >= 0) {
+		const long long idx	 = j - lane;
+		std::uint32_t	v	 = kIdent;
+		bool			incl = true;
+		bool			bad	 = false;
+		if (idx >= 0) {
+			const std::uint32_t s = wait_status(&tiles[idx].st1, epoch, res);
+			if (s == 0) {
+				bad = true;
+			} else {
+				incl = (s & 3u) == kFlagIncl;
+				v	 = incl ? ld_relaxed(&tiles[idx].inc1) : ld_relaxed(&tiles[idx].agg1);
+			}
+		}
+		if (__any_sync(kFull, bad)) {
+			fail = true;
+			return kIdent;
+		}
+		const std::uint32_t ib	  = __ballot_sync(kFull, incl);
+		const int			first = __ffs(ib) - 1;
+		if (ib && lane > first)
+			v = kIdent;
+#pragma unroll
+		for (int off = 1; off < 32; off <<= 1) {
+			const std::uint32_t o = __shfl_down_sync(kFull, v, off);
+			if (lane + off < 32)
+				v = compose_fast(o, v);
+		}
+		v	 = __shfl_sync(kFull, v, 0);
+		excl = compose_fast(v, excl);
+		if (ib)
+			break;
+		j -= 32;
+	}
+	return excl;
+}
+
+// Chain 1 (generic maps).
+__device__ void lookback_maps(TileDescG* tiles, unsigned long long t, std::uint32_t epoch,
+							  DevResult* res, int lane, int nd, std::uint32_t* excl, bool& fail) {
+	for (int d = 0; d < 8; ++d) excl[d] = kIdentMap;
+	long long j = static_cast<long long>(t) - 1;
+	while (j >= 0) {
+		const long long idx	 = j - lane;
+		std::uint32_t	v[8];
+		bool			incl = true;
+		bool			bad	 = false;
+#pragma unroll
+		for (int d = 0; d < 8; ++d) v[d] = kIdentMap;
+		if (idx >= 0) {
+			const std::uint32_t s = wait_status(&tiles[idx].st1, epoch, res);
+			if (s == 0) {
+				bad = true;
+			} else {
+				incl					= (s & 3u) == kFlagIncl;
+				const std::uint32_t* src = incl ? tiles[idx].inc1 : tiles[idx].agg1;
+				for (int d = 0; d < nd; ++d) v[d] = ld_relaxed(src + d);
+			}
+		}
+		if (__any_sync(kFull, bad)) {
+			fail = true;
+			return;
+		}
+		const std::uint32_t ib	  = __ballot_sync(kFull, incl);
+		const int			first = __ffs(ib) - 1;
+		if (ib && lane > first)
+			for (int d = 0; d < 8; ++d) v[d] = kIdentMap;
+		for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+			for (int d = 0; d < 8; ++d) {
+				const std::uint32_t o = __shfl_down_sync(kFull, v[d], off);
+				if (lane + off < 32 && d < nd)
+					v[d] = compose_map(o, v[d]);
+			}
+		}
+#pragma unroll
+		for (int d = 0; d < 8; ++d) {
+			const std::uint32_t w = __shfl_sync(kFull, v[d], 0);
+			if (d < nd)
+				excl[d] = compose_map(w, excl[d]);
+		}
+		if (ib)
+			break;
+		j -= 32;
+	}
+}
+
+// Chain 2 (counts): exclusive sums of tiles [0, t).
+template<class Desc>
+__device__ void lookback_counts(Desc* tiles, unsigned long long t, std::uint32_t epoch,
+								DevResult* res, int lane, unsigned long long* out, bool& fail) {
+	unsigned long long acc[3] = {0, 0, 0};
+	long long		   j	  = static_cast<long long>(t) - 1;
+	while (j >= 0) {
+		const long long	   idx	= j - lane;
+		unsigned long long v[3] = {0, 0, 0};
+		bool			   incl = true;
+		bool			   bad	= false;
+		if (idx >= 0) {
+			const std::uint32_t s = wait_status(&tiles[idx].st2, epoch, res);
+			if (s == 0) {
+				bad = true;
+			} else {
+				incl							= (s & 3u) == kFlagIncl;
+				const std::uint64_t* src = incl ? tiles[idx].inc2 : tiles[idx].agg2;
+				for (int k = 0; k < 3; ++k) v[k] = ld_relaxed64(src + k);
+			}
+		}
+		if (__any_sync(kFull, bad)) {
+			fail = true;
+			return;
+		}
+		const std::uint32_t ib	  = __ballot_sync(kFull, incl);
+		const int			first = __ffs(ib) - 1;
+		if (ib && lane > first)
+			v[0] = v[1] = v[2] = 0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k) {
+			unsigned long long x = v[k];
+#pragma unroll
+			for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(kFull, x, off);
+			acc[k] += __shfl_sync(kFull, x, 0);
+		}
+		if (ib)
+			break;
+		j -= 32;
+	}
+	out[0] = acc[0];
+	out[1] = acc[1];
+	out[2] = acc[2];
+}
+
+// ---- R1: classify 32 bytes through the replicated table ---------------------------
+// tbl_lane: byte address (shared window) of column `lane` of the table.
+__device__ __forceinline__ void classify32(const std::uint32_t (&r)[8], std::uint32_t tbl_lane,
+										   std::uint32_t& S, std::uint32_t& O, std::uint32_t& C,
+										   std::uint32_t& D) {
+	std::uint32_t acc[4];
+#pragma unroll
+	for (int g = 0; g < 4; ++g) {
+		std::uint32_t a = 0;
+#pragma unroll
+		for (int jj = 0; jj < 8; ++jj) {
+			const int			j	= g * 8 + jj;
+			const std::uint32_t w	= r[j >> 2];
+			const int			k	= j & 3;
+			std::uint32_t		off = (k == 0) ? (w << 7) : (w >> (8 * k - 7));
+			off						= (off & 0x7F80u) + tbl_lane;
+			std::uint32_t v;
+			asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(off));
+			a += v << jj;
+		}
+		acc[g] = a;
+	}
+	// 4x4 byte transpose: byte f of acc[g] holds flag plane f for bytes 8g..8g+7.
+	const std::uint32_t t0 = prmt(acc[0], acc[1], 0x5140);
+	const std::uint32_t t1 = prmt(acc[0], acc[1], 0x7362);
+	const std::uint32_t t2 = prmt(acc[2], acc[3], 0x5140);
+	const std::uint32_t t3 = prmt(acc[2], acc[3], 0x7362);
+	S					   = prmt(t0, t2, 0x5410);
+	O					   = prmt(t0, t2, 0x7632);
+	C					   = prmt(t1, t3, 0x5410);
+	D					   = prmt(t1, t3, 0x7632);
+}
+
+// Exact SWAR byte-equality of 32 bytes against a replicated byte; 1 bit per byte.
+__device__ __forceinline__ std::uint32_t eq_mask32(const std::uint32_t (&r)[8], std::uint32_t rep) {
+	std::uint32_t m = 0;
+#pragma unroll
+	for (int i = 0; i < 8; ++i) {
+		const std::uint32_t t = r[i] ^ rep;
+		const std::uint32_t y = (t & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+		const std::uint32_t z = ~(y | t) & 0x80808080u;
+		m |= ((z * 0x00204081u) >> 28) << (4 * i);
+	}
+	return m;
+}
+
+// Loads this thread's 32-byte word from the stage (the two 16-byte halves are read
+// in swapped order on alternate quarter-warps so the LDS.128 phases hit all banks).
+__device__ __forceinline__ void load_word(const unsigned char* stage, int tid, std::uint32_t (&r)[8]) {
+	const int	 sw = (tid >> 2) & 1;
+	const uint4* p	= reinterpret_cast<const uint4*>(stage + 32 * tid);
+	const uint4	 x	= p[sw];
+	const uint4	 y	= p[sw ^ 1];
+	const uint4	 h0 = sw ? y : x;
+	const uint4	 h1 = sw ? x : y;
+	r[0] = h0.x;
+	r[1] = h0.y;
+	r[2] = h0.z;
+	r[3] = h0.w;
+	r[4] = h1.x;
+	r[5] = h1.y;
+	r[6] = h1.z;
+	r[7] = h1.w;
+}
+
+template<class T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+	for (int off = 16; off > 0; off >>= 1) {
+		const T o = __shfl_xor_sync(kFull, v, off);
+		v		  = o < v ? o : v;
+	}
+	return v;
+}
+
+template<class T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+	for (int off = 16; off > 0; off >>= 1) {
+		const T o = __shfl_xor_sync(kFull, v, off);
+		v		  = o > v ? o : v;
+	}
+	return v;
+}
+
+// Shared-memory layout of the scan kernels.
+struct SmemLayout {
+	static constexpr int kTbl	  = 0;
+	static constexpr int kStage	  = kTbl + kTableBytes;
+	static constexpr int kBars	  = kStage + kStages * kTileBytes;
+	static constexpr int kScratch = kBars + 64;
+	static constexpr int kHist	  = (kScratch + static_cast<int>(sizeof(Scratch)) + 127) & ~127;
+	static constexpr int kGen	  = kHist + 2 * kKeyWindow * 4;	 // generic: rep_of + step tables
+	static constexpr int kBytesFast = kGen;
+	static constexpr int kBytesGen	= kGen + 8 * 256 + 8 * 64 + 2 * 8 * 8 * 4;
+};
+
+// First tile of a scan initialises the result block (and, for the first chunk of
+// a document, the running depth extrema and key histogram) before it publishes,
+// so every other tile's atomics on them happen after.
+__device__ __forceinline__ void init_result(DevResult* res, int path, bool first_chunk) {
+	if (first_chunk) {
+		res->min_bal = 0;
+		res->max_bal = 0;
+		res->min_key = 0x7FFFFFFFFFFFFFFFll;
+		res->max_key = -0x7FFFFFFFFFFFFFFFll;
+		res->keys_oob = 0;
+	}
+	res->unclosed  = 0;
+	res->spec_fail = 0;
+	res->mismatch  = 0;
+	res->sort_ok   = 0;
+	res->path	   = path;
+}
+
+}  // namespace
+
+// ============================================================================
+// The scan kernel.  PATH selects the R4 algebra; everything else is shared.
+// ============================================================================
+template<int PATH>
+__global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
+	extern __shared__ __align__(128) unsigned char smem[];
+	std::uint32_t*	 tbl	= reinterpret_cast<std::uint32_t*>(smem + SmemLayout::kTbl);
+	unsigned char*	 stages = smem + SmemLayout::kStage;
+	std::uint64_t*	 bars	= reinterpret_cast<std::uint64_t*>(smem + SmemLayout::kBars);
+	Scratch&		 sc		= *reinterpret_cast<Scratch*>(smem + SmemLayout::kScratch);
+	unsigned int*	 khist	= reinterpret_cast<unsigned int*>(smem + SmemLayout::kHist);
+	std::uint8_t*	 g_rep	= smem + SmemLayout::kGen;					   // [8][256]
+	std::uint8_t*	 g_step = g_rep + 8 * 256;							   // [8][8][8]
+	std::uint32_t*	 g_tlo	= reinterpret_cast<std::uint32_t*>(g_step + 8 * 64);  // [8][8]
+	std::uint32_t*	 g_thi	= g_tlo + 64;
+
+	const int			tid	 = threadIdx.x;
+	const int			lane = tid & 31;
+	const int			warp = tid >> 5;
+	const DevPlan*		P	 = a.plan;
+	DevResult*			res	 = a.res;
+	const bool			brk	 = P->has_brackets != 0;
+	const int			nd	 = P->n_descs;
+
+	// ---- one-time CTA set-up: replicated class table, generic tables ----------
+	for (int i = tid; i < 256 * 32; i += kScanThreads) tbl[i] = P->cls[i >> 5];
+	if (brk)
+		for (int i = tid; i < 2 * kKeyWindow; i += kScanThreads) khist[i] = 0;
+	if (PATH == kPathGeneric) {
+		for (int i = tid; i < 8 * 256; i += kScanThreads) g_rep[i] = (&P->rep_of[0][0])[i];
+		for (int i = tid; i < 8 * 64; i += kScanThreads) g_step[i] = (&P->step[0][0][0])[i];
+		for (int i = tid; i < 64; i += kScanThreads) {
+			g_tlo[i] = (&P->tb_lo[0][0])[i];
+			g_thi[i] = (&P->tb_hi[0][0])[i];
+		}
+	}
+	if (tid == 0) {
+		for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+		fence_barrier_init();
+		sc.failed = 0;
+	}
+	__syncthreads();
+
+	std::uint32_t pending = 0;	// tid 0: stages with a bulk copy in flight
+	auto issue = [&](int s) {  // tid 0 only: take a ticket and start its copy
+		const unsigned long long t = atomicAdd(&a.ctr->scan_ticket, 1u);
+		sc.tile_id[s]			   = t;
+		if (t < a.ntiles) {
+			pending |= 1u << s;
+			const unsigned long long off   = t * kTileBytes;
+			unsigned long long		 bytes = a.copy_end - off;
+			if (bytes > kTileBytes)
+				bytes = kTileBytes;
+			mbar_arrive_expect_tx(&bars[s], static_cast<std::uint32_t>(bytes));
+			bulk_g2s(stages + s * kTileBytes, a.base + off, static_cast<std::uint32_t>(bytes),
+					 &bars[s]);
+		}
+	};
+	if (tid == 0)
+		for (int s = 0; s < kStages; ++s) issue(s);
+	__syncthreads();
+
+	const std::uint32_t tbl_lane = smem_addr(tbl) + 4u * lane;
+	const std::uint32_t escape_rep = P->escape_rep;
+	const std::uint8_t	delim	   = P->delim;
+	const std::uint32_t epoch	 = a.epoch & 0x3FFFFFFFu;
+	const unsigned long long doc_end = a.o + a.n;  // stream position one past the last byte
+	const unsigned long long byte_base = a.carry_in ? a.carry_in->byte_base : 0ull;
+	const bool first_chunk = byte_base == 0;
+	long long my_min_bal = 0, my_max_bal = 0, my_min_key = 0x7FFFFFFFFFFFFFFFll,
+			  my_max_key = -0x7FFFFFFFFFFFFFFFll;
+	bool any_keys = false;
+
+	std::uint32_t phase_bits = 0;
+	for (int it = 0;; ++it) {
+		const int				 s = it % kStages;
+		const unsigned long long t = sc.tile_id[s];
+		if (t >= a.ntiles)
+			break;
+		// wait for the tile's bytes
+		{
+			std::uint32_t spins = 0;
+			const std::uint32_t ph = (phase_bits >> s) & 1u;
+			while (!mbar_try_wait(&bars[s], ph)) {
+				if (++spins > kSpinLimit) {
+					record_error(res, kDevErrTimeout);
+					sc.failed = 1;
+					break;
+				}
+			}
+			phase_bits ^= 1u << s;
+			pending &= ~(1u << s);
+		}
+		const unsigned char*	 stage = stages + s * kTileBytes;
+		const unsigned long long q0	   = t * kTileBytes + 32ull * tid;	// stream pos of word
+		int lo = 0, hi = 32;
+		if (q0 < a.o)
+			lo = static_cast<int>(a.o - q0) > 32 ? 32 : static_cast<int>(a.o - q0);
+		if (doc_end < q0 + 32)
+			hi = doc_end <= q0 ? 0 : static_cast<int>(doc_end - q0);
+		if (hi < lo)
+			hi = lo;
+		const std::uint32_t vm = bit_range(lo, hi);
+
+		// ---- R1 ---------------------------------------------------------------
+		std::uint32_t r[8];
+		load_word(stage, tid, r);
+		std::uint32_t S, O, C, D;
+		classify32(r, tbl_lane, S, O, C, D);
+		S &= vm;
+		O &= vm;
+		C &= vm;
+		D &= vm;
+
+		// ---- R4 (local): element of this word -----------------------------------
+		std::uint32_t elem = kIdent;
+		std::uint32_t B = 0, esc0 = 0, fbit = 0;
+		std::uint32_t gmap[8];
+		if (PATH == kPathParity || PATH == kPathDoubled) {
+			elem = 1u | ((__popc(D) & 1u) << 2);
+		} else if (PATH == kPathEscape) {
+			B							= eq_mask32(r, escape_rep) & vm;
+			const std::uint32_t runs	= B & ~(B << 1);
+			const std::uint32_t se		= runs & 0x55555555u;
+			const std::uint32_t so		= runs & 0xAAAAAAAAu;
+			const std::uint32_t ee		= (B + se) & ~B;
+			const std::uint32_t eo		= (B + so) & ~B;
+			esc0						= (ee & 0xAAAAAAAAu) | (eo & 0x55555555u);
+			const std::uint32_t nbv		= ~B & vm;
+			fbit						= nbv & (0u - nbv);	 // lowest valid non-backslash
+			if (vm != 0) {
+				const std::uint32_t bt = hi >= 32 ? B : (B << (32 - hi));
+				const std::uint32_t L  = __clz(~bt);
+				const std::uint32_t aa = nbv == 0 ? 1u : 0u;
+				const std::uint32_t bb = L & 1u;
+				const std::uint32_t qq = __popc(D & ~esc0) & 1u;
+				const std::uint32_t dd = (D & fbit) ? 1u : 0u;
+				elem				   = aa | (bb << 1) | (qq << 2) | (dd << 3);
+			}
+		} else if (PATH == kPathGeneric) {
+			for (int d = 0; d < 8; ++d) gmap[d] = kIdentMap;
+			const unsigned char* wb = stage + 32 * tid;
+			for (int d = 0; d < nd; ++d) {
+				std::uint32_t m = kIdentMap;
+				for (int j = lo; j < hi; ++j) {
+					const int cl = g_rep[d * 256 + wb[j]];
+					m			 = then_map(m, g_tlo[d * 8 + cl], g_thi[d * 8 + cl]);
+				}
+				gmap[d] = m;
+			}
+		}
+
+		// ---- chain 1: block scan + look-back ---------------------------------------
+		std::uint32_t excl_elem = kIdent;  // thread's exclusive element within the tile
+		std::uint32_t gexcl[8];
+		if (PATH != kPathNone && PATH != kPathGeneric) {
+			std::uint32_t v = elem;
+#pragma unroll
+			for (int off = 1; off < 32; off <<= 1) {
+				const std::uint32_t o = __shfl_up_sync(kFull, v, off);
+				if (lane >= off)
+					v = compose_fast(o, v);
+			}
+			excl_elem = __shfl_up_sync(kFull, v, 1);
+			if (lane == 0)
+				excl_elem = kIdent;
+			if (lane == 31)
+				sc.warp_elem[warp] = v;
+		} else if (PATH == kPathGeneric) {
+			for (int d = 0; d < 8; ++d) {
+				std::uint32_t v = gmap[d];
+#pragma unroll
+				for (int off = 1; off < 32; off <<= 1) {
+					const std::uint32_t o = __shfl_up_sync(kFull, v, off);
+					if (lane >= off && d < nd)
+						v = compose_map(o, v);
+				}
+				std::uint32_t e = __shfl_up_sync(kFull, v, 1);
+				gexcl[d]		= lane == 0 ? kIdentMap : e;
+				if (lane == 31)
+					sc.warp_maps[warp][d] = v;
+			}
+		}
+		__syncthreads();
+		if (warp == 0) {
+			bool fail = false;
+			if (PATH != kPathNone && PATH != kPathGeneric) {
+				// warp-exclusive prefix of the 16 warp aggregates
+				std::uint32_t w = lane < 16 ? sc.warp_elem[lane] : kIdent;
+				std::uint32_t v = w;
+#pragma unroll
+				for (int off = 1; off < 16; off <<= 1) {
+					const std::uint32_t o = __shfl_up_sync(kFull, v, off);
+					if (lane >= off)
+						v = compose_fast(o, v);
+				}
+				const std::uint32_t agg = __shfl_sync(kFull, v, 15);
+				std::uint32_t		we	= __shfl_up_sync(kFull, v, 1);
+				if (lane == 0)
+					we = kIdent;
+				TileDesc* tiles = static_cast<TileDesc*>(a.tiles);
+				std::uint32_t texcl = kIdent;
+				if (t > 0) {
+					if (lane == 0) {
+						tiles[t].agg1 = agg;
+						st_release(&tiles[t].st1, (epoch << 2) | kFlagAgg);
+					}
+					texcl = lookback_fast(tiles, t, epoch, res, lane, fail);
+				}
+				if (lane == 0) {
+					if (t == 0)
+						sc.init_state = a.carry_in ? a.carry_in->fstate : 0u;
+					tiles[t].inc1 = compose_fast(texcl, agg);
+					if (t == 0)
+						init_result(res, PATH, first_chunk);
+				}
+				if (t == 0 && brk && first_chunk)
+					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
+				__syncwarp();
+				if (lane == 0)
+					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
+				if (lane < 16)
+					sc.warp_elem[lane] = compose_fast(texcl, we);	// tile-exclusive per warp
+			} else if (PATH == kPathGeneric) {
+				TileDescG*	  tiles = static_cast<TileDescG*>(a.tiles);
+				std::uint32_t we[8], agg[8], texcl[8];
+				for (int d = 0; d < 8; ++d) {
+					const std::uint32_t w = lane < 16 ? sc.warp_maps[lane][d] : kIdentMap;
+					std::uint32_t		v = w;
+#pragma unroll
+					for (int off = 1; off < 16; off <<= 1) {
+						const std::uint32_t o = __shfl_up_sync(kFull, v, off);
+						if (lane >= off && d < nd)
+							v = compose_map(o, v);
+					}
+					agg[d]			= __shfl_sync(kFull, v, 15);
+					std::uint32_t e = __shfl_up_sync(kFull, v, 1);
+					we[d]			= lane == 0 ? kIdentMap : e;
+					texcl[d]		= kIdentMap;
+				}
+				if (t > 0) {
+					if (lane == 0) {
+						for (int d = 0; d < nd; ++d) tiles[t].agg1[d] = agg[d];
+						st_release(&tiles[t].st1, (epoch << 2) | kFlagAgg);
+					}
+					lookback_maps(tiles, t, epoch, res, lane, nd, texcl, fail);
+				}
+				if (lane == 0) {
+					for (int d = 0; d < nd; ++d) tiles[t].inc1[d] = compose_map(texcl[d], agg[d]);
+					if (t == 0) {
+						for (int d = 0; d < 8; ++d)
+							sc.init_gstate[d] = a.carry_in ? a.carry_in->gstate[d]
+														   : (d < nd ? P->start[d] : 0u);
+						init_result(res, PATH, first_chunk);
+					}
+				}
+				if (t == 0 && brk && first_chunk)
+					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
+				__syncwarp();
+				if (lane == 0)
+					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
+				if (lane < 16)
+					for (int d = 0; d < nd; ++d) sc.warp_maps[lane][d] = compose_map(texcl[d], we[d]);
+			} else {  // kPathNone: still publish so the structure is uniform
+				if (lane == 0 && t == 0)
+					init_result(res, PATH, first_chunk);
+				if (t == 0 && brk && first_chunk)
+					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
+			}
+			if (fail && lane == 0)
+				sc.failed = 1;
+		}
+		__syncthreads();
+		if (sc.failed)
+			break;
+
+		// ---- R4 (resolve) + R3: per-byte masked bitmap ---------------------------
+		std::uint32_t mask = 0, endstate = 0, last_flag = 0;
+		std::uint32_t gend[8];
+		if (PATH == kPathParity || PATH == kPathDoubled || PATH == kPathEscape) {
+			// state at this word's first byte
+			const std::uint32_t pre = compose_fast(sc.warp_elem[warp], excl_elem);
+			// tile 0 publishes init via smem; other tiles read carry directly
+			const std::uint32_t init = a.carry_in ? a.carry_in->fstate : 0u;
+			const std::uint32_t st	 = apply_fast(pre, init);
+			const std::uint32_t e_in = st & 1u, p_in = (st >> 1) & 1u;
+			std::uint32_t		tog = D;
+			std::uint32_t		esc = 0;
+			if (PATH == kPathEscape) {
+				esc = esc0 ^ (e_in ? fbit : 0u);
+				tog = D & ~esc;
+			}
+			const std::uint32_t incl = prefix_xor32(tog);
+			std::uint32_t		ex	 = incl ^ tog;
+			if (p_in)
+				ex = ~ex;
+			mask = ex & vm;
+			if (PATH == kPathDoubled) {
+				// Was the byte before each byte a delimiter?  Inside the word that is
+				// D << 1; the byte before bit `lo` comes from the previous word, the
+				// previous tile, or (at the document/chunk start) the carry.
+				std::uint32_t prev = __shfl_up_sync(kFull, D >> 31, 1);
+				const bool	  first = (q0 + lo == a.o);	 // word holds the first byte
+				if (first) {
+					prev = a.carry_in ? (a.carry_in->last_delim & 1u) : 0u;
+				} else if (lane == 0 && vm != 0) {
+					// lo == 0 and q0 > o here: the previous byte is a document byte
+					prev = (tid > 0 ? stage[32 * tid - 1] : a.base[q0 - 1]) == delim ? 1u : 0u;
+				}
+				const std::uint32_t dprev = (D << 1) | ((prev & 1u) << lo);
+				mask |= D & dprev;
+				mask &= vm;
+			}
+			if (PATH == kPathEscape) {
+				if (D & esc & ~mask & vm)
+					atomicOr(&res->spec_fail, 1u);
+			}
+			if (hi > lo && doc_end <= q0 + 32 && doc_end > q0) {
+				// this word holds the last byte of the document/chunk
+				endstate				  = apply_fast(elem, st);
+				const std::uint32_t lastb = 1u << (hi - 1);
+				last_flag				  = (PATH == kPathEscape) ? ((tog & lastb) ? 1u : 0u)
+																  : ((D & lastb) ? 1u : 0u);
+			}
+		} else if (PATH == kPathGeneric) {
+			const unsigned char* wb = stage + 32 * tid;
+			for (int d = 0; d < nd; ++d) {
+				const std::uint32_t pre	  = compose_map(sc.warp_maps[warp][d], gexcl[d]);
+				const std::uint32_t init  = a.carry_in ? a.carry_in->gstate[d] : P->start[d];
+				std::uint32_t		stt	  = (pre >> (4 * init)) & 0xFu;
+				for (int j = lo; j < hi; ++j) {
+					const int			cl = g_rep[d * 256 + wb[j]];
+					const std::uint32_t x  = g_step[d * 64 + stt * 8 + cl];
+					mask |= ((x >> 3) & 1u) << j;
+					stt = x & 7u;
+				}
+				gend[d] = stt;
+			}
+			mask &= vm;
+		}
+
+		// ---- R2/R3 select + chain 2 counts -------------------------------------------
+		const std::uint32_t sel	 = S & ~mask;
+		const std::uint32_t selo = O & ~mask;
+		const std::uint32_t selc = C & ~mask;
+		std::uint32_t		c0 = __popc(sel), c1 = __popc(selo), c2 = __popc(selc);
+		std::uint32_t		x0 = c0, x1 = c1, x2 = c2;
+#pragma unroll
+		for (int off = 1; off < 32; off <<= 1) {
+			const std::uint32_t y0 = __shfl_up_sync(kFull, x0, off);
+			const std::uint32_t y1 = __shfl_up_sync(kFull, x1, off);
+			const std::uint32_t y2 = __shfl_up_sync(kFull, x2, off);
+			if (lane >= off) {
+				x0 += y0;
+				x1 += y1;
+				x2 += y2;
+			}
+		}
+		if (lane == 31) {
+			sc.warp_cnt[warp][0] = x0;
+			sc.warp_cnt[warp][1] = x1;
+			sc.warp_cnt[warp][2] = x2;
+		}
+		x0 -= c0;
+		x1 -= c1;
+		x2 -= c2;
+		__syncthreads();
+		if (warp == 0) {
+			std::uint32_t w0 = lane < 16 ? sc.warp_cnt[lane][0] : 0u;
+			std::uint32_t w1 = lane < 16 ? sc.warp_cnt[lane][1] : 0u;
+			std::uint32_t w2 = lane < 16 ? sc.warp_cnt[lane][2] : 0u;
+			std::uint32_t v0 = w0, v1 = w1, v2 = w2;
+#pragma unroll
+			for (int off = 1; off < 16; off <<= 1) {
+				const std::uint32_t y0 = __shfl_up_sync(kFull, v0, off);
+				const std::uint32_t y1 = __shfl_up_sync(kFull, v1, off);
+				const std::uint32_t y2 = __shfl_up_sync(kFull, v2, off);
+				if (lane >= off) {
+					v0 += y0;
+					v1 += y1;
+					v2 += y2;
+				}
+			}
+			const unsigned long long tot[3] = {__shfl_sync(kFull, v0, 15), __shfl_sync(kFull, v1, 15),
+											   __shfl_sync(kFull, v2, 15)};
+			unsigned long long base[3]	  = {0, 0, 0};
+			bool			   fail		  = false;
+			if (PATH == kPathGeneric) {
+				TileDescG* tiles = static_cast<TileDescG*>(a.tiles);
+				if (t > 0) {
+					if (lane == 0) {
+						for (int k = 0; k < 3; ++k) tiles[t].agg2[k] = tot[k];
+						st_release(&tiles[t].st2, (epoch << 2) | kFlagAgg);
+					}
+					lookback_counts(tiles, t, epoch, res, lane, base, fail);
+				} else if (a.carry_in) {
+					base[0] = a.carry_in->ns;
+					base[1] = a.carry_in->no;
+					base[2] = a.carry_in->nc;
+				}
+				if (lane == 0) {
+					for (int k = 0; k < 3; ++k) tiles[t].inc2[k] = base[k] + tot[k];
+					st_release(&tiles[t].st2, (epoch << 2) | kFlagIncl);
+				}
+			} else {
+				TileDesc* tiles = static_cast<TileDesc*>(a.tiles);
+				if (t > 0) {
+					if (lane == 0) {
+						for (int k = 0; k < 3; ++k) tiles[t].agg2[k] = tot[k];
+						st_release(&tiles[t].st2, (epoch << 2) | kFlagAgg);
+					}
+					lookback_counts(tiles, t, epoch, res, lane, base, fail);
+				} else if (a.carry_in) {
+					base[0] = a.carry_in->ns;
+					base[1] = a.carry_in->no;
+					base[2] = a.carry_in->nc;
+				}
+				if (lane == 0) {
+					for (int k = 0; k < 3; ++k) tiles[t].inc2[k] = base[k] + tot[k];
+					st_release(&tiles[t].st2, (epoch << 2) | kFlagIncl);
+				}
+			}
+			if (lane < 16) {
+				sc.warp_cnt[lane][0] = v0 - w0;
+				sc.warp_cnt[lane][1] = v1 - w1;
+				sc.warp_cnt[lane][2] = v2 - w2;
+			}
+			if (lane == 0) {
+				sc.base_cnt[0] = base[0];
+				sc.base_cnt[1] = base[1];
+				sc.base_cnt[2] = base[2];
+				if (fail)
+					sc.failed = 1;
+				if (t == a.ntiles - 1) {
+					res->n_struct	= base[0] + tot[0];
+					res->n_open		= base[1] + tot[1];
+					res->n_close	= base[2] + tot[2];
+					res->n_brackets = res->n_open + res->n_close;
+					if (a.carry_out) {
+						a.carry_out->ns		   = base[0] + tot[0];
+						a.carry_out->no		   = base[1] + tot[1];
+						a.carry_out->nc		   = base[2] + tot[2];
+						a.carry_out->byte_base = byte_base + a.n;
+					}
+				}
+			}
+		}
+		__syncthreads();
+		if (sc.failed)
+			break;
+
+		// ---- end-of-document state (the thread holding the last byte) -----------
+		if (hi > lo && doc_end <= q0 + 32 && doc_end > q0) {
+			std::uint32_t unclosed = 0;
+			if (PATH == kPathParity || PATH == kPathDoubled || PATH == kPathEscape) {
+				unclosed = ((endstate >> 1) & 1u) | last_flag;
+				if (a.carry_out) {
+					a.carry_out->fstate		 = endstate;
+					a.carry_out->last_delim	 = (D >> (hi - 1)) & 1u;
+					a.carry_out->last_toggle = last_flag;
+				}
+			} else if (PATH == kPathGeneric) {
+				for (int d = 0; d < nd; ++d)
+					if (gend[d] != P->start[d])
+						unclosed = 1;
+				if (a.carry_out)
+					for (int d = 0; d < 8; ++d) a.carry_out->gstate[d] = d < nd ? gend[d] : 0u;
+			}
+			res->unclosed = unclosed;
+			if (a.carry_out)
+				a.carry_out->unclosed = unclosed;
+		}
+
+		// ---- R5: write outputs -----------------------------------------------------
+		{
+			unsigned long long si = sc.base_cnt[0] + sc.warp_cnt[warp][0] + x0;
+			const unsigned long long no0 = sc.base_cnt[1] + sc.warp_cnt[warp][1] + x1;
+			const unsigned long long nc0 = sc.base_cnt[2] + sc.warp_cnt[warp][2] + x2;
+			unsigned long long		 bi	 = no0 + nc0;
+			long long				 dep = static_cast<long long>(no0) - static_cast<long long>(nc0);
+			const unsigned long long pos0 = byte_base + q0 - a.o;  // position of bit 0
+			const unsigned char*	 wb	  = stage + 32 * tid;
+			const bool want_pairs = (a.flags & 1u) != 0;
+			const bool want_chars = (a.flags & 4u) != 0;
+			std::uint32_t			 m	  = sel;
+			const std::uint32_t		 bm	  = selo | selc;
+			while (m) {
+				const int j = __ffs(m) - 1;
+				m &= m - 1;
+				const std::uint32_t pos = static_cast<std::uint32_t>(pos0 + j);
+				if (si < a.cap_s) {
+					a.pos[si] = pos;
+					if (want_chars)
+						a.chars[si] = wb[j];
+				}
+				if ((bm >> j) & 1u) {
+					const bool op  = (selo >> j) & 1u;
+					const long long key = op ? dep : dep - 1;
+					dep += op ? 1 : -1;
+					if (bi < a.cap_b) {
+						a.bpos[bi]	= pos;
+						a.bchar[bi] = wb[j];
+						a.bsi[bi]	= static_cast<std::uint32_t>(si);
+						a.depth[bi] = static_cast<std::int32_t>(key);
+					}
+					++bi;
+					my_min_bal = dep < my_min_bal ? dep : my_min_bal;
+					my_max_bal = dep > my_max_bal ? dep : my_max_bal;
+					my_min_key = key < my_min_key ? key : my_min_key;
+					my_max_key = key > my_max_key ? key : my_max_key;
+					any_keys   = true;
+					if (key >= -kKeyWindow && key < kKeyWindow)
+						atomicAdd(&khist[key + kKeyWindow], 1u);
+					else
+						atomicOr(&res->keys_oob, 1u);
+				} else if (want_pairs && si < a.cap_s) {
+					a.pair[si] = -1;
+				}
+				++si;
+			}
+			if ((a.flags & 8u) && a.mask && lo < hi) {
+				// mask output needs a 32-byte aligned word grid (o == 0)
+				const unsigned long long wi = (byte_base + q0 - a.o) >> 5;
+				a.mask[wi]					= mask;
+			}
+		}
+
+		// ---- stage consumed: refill it ------------------------------------------------
+		__syncthreads();
+		if (tid == 0)
+			issue(s);
+		__syncthreads();
+	}
+
+	// ---- after a failure, drain this CTA's bulk copies still in flight -----------------
+	if (tid == 0 && pending) {
+		for (int s = 0; s < kStages; ++s) {
+			if (!(pending & (1u << s)))
+				continue;
+			std::uint32_t spins = 0;
+			while (!mbar_try_wait(&bars[s], (phase_bits >> s) & 1u) && ++spins < kSpinLimit) {
+			}
+		}
+	}
+
+	// ---- CTA exit: flush depth extrema and the key histogram ---------------------------
+	if (brk) {
+		const long long v0 = warp_min(my_min_bal), v1 = warp_max(my_max_bal);
+		const long long v2 = warp_min(my_min_key), v3 = warp_max(my_max_key);
+		const bool		anyk = __any_sync(kFull, any_keys);
+		if (lane == 0) {
+			sc.wmin_bal[warp] = v0;
+			sc.wmax_bal[warp] = v1;
+			sc.wmin_key[warp] = v2;
+			sc.wmax_key[warp] = v3;
+		}
+		if (tid == 0)
+			sc.any_br = 0;
+		__syncthreads();
+		if (lane == 0 && anyk)
+			atomicOr(&sc.any_br, 1u);
+		__syncthreads();
+		if (tid == 0 && sc.any_br && !sc.failed) {
+			long long mn = 0, mx = 0, kn = 0x7FFFFFFFFFFFFFFFll, kx = -0x7FFFFFFFFFFFFFFFll;
+			for (int w = 0; w < kScanThreads / 32; ++w) {
+				mn = sc.wmin_bal[w] < mn ? sc.wmin_bal[w] : mn;
+				mx = sc.wmax_bal[w] > mx ? sc.wmax_bal[w] : mx;
+				kn = sc.wmin_key[w] < kn ? sc.wmin_key[w] : kn;
+				kx = sc.wmax_key[w] > kx ? sc.wmax_key[w] : kx;
+			}
+			atomicMin(&res->min_bal, mn);
+			atomicMax(&res->max_bal, mx);
+			atomicMin(&res->min_key, kn);
+			atomicMax(&res->max_key, kx);
+		}
+		if (sc.any_br && !sc.failed)
+			for (int i = tid; i < 2 * kKeyWindow; i += kScanThreads)
+				if (khist[i])
+					atomicAdd(&a.key_hist[i], khist[i]);
+	}
+	// ---- last CTA out resets the tickets for the next launch ------------------------
+	__syncthreads();
+	if (tid == 0) {
+		__threadfence();
+		const unsigned int done = atomicAdd(&a.ctr->scan_done, 1u);
+		if (done == gridDim.x - 1) {
+			a.ctr->scan_ticket = 0;
+			a.ctr->scan_done   = 0;
+			__threadfence();
+		}
+	}
+}
+
+template __global__ void k_scan<kPathNone>(const ScanArgs);
+template __global__ void k_scan<kPathParity>(const ScanArgs);
+template __global__ void k_scan<kPathDoubled>(const ScanArgs);
+template __global__ void k_scan<kPathEscape>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric>(const ScanArgs);
+
+int scan_smem_bytes(int path) {
+	return path == kPathGeneric ? SmemLayout::kBytesGen : SmemLayout::kBytesFast;
+}
+
+const void* scan_kernel(int path) {
+	switch (path) {
+		case kPathNone: return reinterpret_cast<const void*>(&k_scan<kPathNone>);
+		case kPathParity: return reinterpret_cast<const void*>(&k_scan<kPathParity>);
+		case kPathDoubled: return reinterpret_cast<const void*>(&k_scan<kPathDoubled>);
+		case kPathEscape: return reinterpret_cast<const void*>(&k_scan<kPathEscape>);
+		default: return reinterpret_cast<const void*>(&k_scan<kPathGeneric>);
+	}
+}
+
+}  // namespace pars

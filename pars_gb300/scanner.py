@@ -1,0 +1,234 @@
+"""Python mirror of the reference backend's public boundary.
+
+``Scanner`` corresponds to ``pars::gpu::scanner<S>``
+(include/pars/backend/cuda/pipeline.cuh:1164-1258) with the plan passed at run time:
+
+* ``scan_device(d_ptr, n, stream, want_pairs, run_pairs)`` — device-resident input,
+  results stay on the device (pipeline.cuh:1166-1173);
+* ``scan_host(data, stream, want_pairs)`` — host input, results copied back
+  (pipeline.cuh:1176-1212);
+* ``reserve_struct`` / ``scan_chunk`` / ``struct_ptr`` — chunked stage 1
+  (pipeline.cuh:1214-1225), here for every plan kind with the carry kept on the device.
+
+Device results are borrowed from the context until its next scan, as in the
+reference; ``DeviceResult.*()`` return zero-copy torch views of those buffers.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import (PARS_FORCE_GENERIC, PARS_RUN_PAIRS, PARS_WANT_CHARS, PARS_WANT_MASK,
+                   PARS_WANT_PAIRS, check, lib)
+
+PATH_NAMES = {0: "none", 1: "parity", 2: "doubled", 3: "escape", 4: "generic"}
+
+
+class _DevArray:
+    """Exposes a raw device pointer through __cuda_array_interface__ (zero copy)."""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {
+            "shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), True),
+            "version": 2, "strides": None,
+        }
+
+
+def _view(ptr, n, typestr, torch_dtype):
+    import torch
+    if not ptr or n == 0:
+        return torch.empty(0, dtype=torch_dtype, device="cuda")
+    return torch.as_tensor(_DevArray(ptr, n, typestr), device="cuda")
+
+
+class DeviceResult:
+    """cf. ``device_result`` (pipeline.cuh:722-728), plus the bracket arrays."""
+
+    def __init__(self, r: _lib.DeviceResult, n_bytes: int):
+        self.raw = r
+        self.n_bytes = n_bytes
+        self.n_struct = int(r.n_struct)
+        self.n_brackets = int(r.n_brackets)
+        self.balanced = bool(r.balanced)
+        self.well_formed = bool(r.well_formed)
+        self.max_depth = int(r.max_depth)
+        self.unclosed_mode = bool(r.unclosed_mode)
+        self.kernel_path = PATH_NAMES.get(int(r.kernel_path), str(r.kernel_path))
+
+    def structural(self):
+        import torch
+        return _view(self.raw.structural, self.n_struct, "<u4", torch.uint32)
+
+    def chars(self):
+        import torch
+        return _view(self.raw.chars, self.n_struct if self.raw.chars else 0, "|u1", torch.uint8)
+
+    def pair_pos(self):
+        import torch
+        return _view(self.raw.pair_pos, self.n_struct if self.raw.pair_pos else 0, "<i4", torch.int32)
+
+    def bracket_pos(self):
+        import torch
+        return _view(self.raw.bracket_pos, self.n_brackets, "<u4", torch.uint32)
+
+    def bracket_char(self):
+        import torch
+        return _view(self.raw.bracket_char, self.n_brackets, "|u1", torch.uint8)
+
+    def bracket_struct(self):
+        import torch
+        return _view(self.raw.bracket_struct, self.n_brackets, "<u4", torch.uint32)
+
+    def depth(self):
+        import torch
+        return _view(self.raw.depth, self.n_brackets, "<i4", torch.int32)
+
+    def bracket_pair(self):
+        import torch
+        n = self.n_brackets if self.raw.bracket_pair else 0
+        return _view(self.raw.bracket_pair, n, "<i4", torch.int32)
+
+    def mask(self):
+        import torch
+        n = (self.n_bytes + 31) // 32 if self.raw.mask else 0
+        return _view(self.raw.mask, n, "<u4", torch.uint32)
+
+    def to_numpy(self) -> dict:
+        """Host copies of every returned array (uint32 arrays come back as uint32)."""
+        def np_(t, dt):
+            return t.cpu().numpy().view(dt) if t.numel() else np.zeros(0, dt)
+        return {
+            "pos": np_(self.structural().view(__import__("torch").int32), np.uint32),
+            "chars": np_(self.chars(), np.uint8),
+            "pair": np_(self.pair_pos(), np.int32),
+            "bpos": np_(self.bracket_pos().view(__import__("torch").int32), np.uint32),
+            "bchar": np_(self.bracket_char(), np.uint8),
+            "bsi": np_(self.bracket_struct().view(__import__("torch").int32), np.uint32),
+            "depth": np_(self.depth(), np.int32),
+            "bpair": np_(self.bracket_pair(), np.int32),
+            "mask": np_(self.mask().view(__import__("torch").int32), np.uint32),
+        }
+
+
+@dataclass
+class HostResult:
+    """cf. ``host_result`` (pipeline.cuh:730-735)."""
+    structural: np.ndarray
+    pair_pos: np.ndarray
+    chars: np.ndarray
+    balanced: bool
+    well_formed: bool
+    max_depth: int
+    unclosed_mode: bool
+
+
+class Context:
+    """A pars_ctx: one device, grow-only buffers, loaded plans (one host thread)."""
+
+    def __init__(self, device: int = 0, arena_bytes: int = 0):
+        self._ctx = ctypes.c_void_p()
+        check(lib().pars_create(device, arena_bytes, ctypes.byref(self._ctx)))
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    def load_plan(self, plan: bytes) -> int:
+        if len(plan) != _lib.PLAN_BYTES:
+            raise ValueError(f"scan_plan must be {_lib.PLAN_BYTES} bytes, got {len(plan)}")
+        buf = ctypes.create_string_buffer(bytes(plan), len(plan))
+        pid = ctypes.c_int()
+        check(lib().pars_plan_load(self._ctx, buf, len(plan), ctypes.byref(pid)), self._ctx)
+        return pid.value
+
+    def plan_path(self, pid: int) -> str:
+        p = ctypes.c_int()
+        check(lib().pars_plan_path(self._ctx, pid, ctypes.byref(p)), self._ctx)
+        return PATH_NAMES[p.value]
+
+    def close(self):
+        if self._ctx:
+            lib().pars_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scanner:
+    """``scanner<S>`` for one plan.  ``plan`` is the raw scan_plan POD (3177 bytes)."""
+
+    def __init__(self, plan: bytes, device: int = 0, ctx: Context | None = None):
+        self.ctx = ctx or Context(device)
+        self.plan_id = self.ctx.load_plan(plan)
+        self.path = self.ctx.plan_path(self.plan_id)
+
+    def scan_device(self, d_ptr: int, n: int, stream: int = 0, want_pairs: bool = False,
+                    run_pairs: bool = True, want_chars: bool = False, want_mask: bool = False,
+                    force_generic: bool = False) -> DeviceResult:
+        flags = ((PARS_WANT_PAIRS if want_pairs else 0) | (PARS_RUN_PAIRS if run_pairs else 0)
+                 | (PARS_WANT_CHARS if want_chars else 0) | (PARS_WANT_MASK if want_mask else 0)
+                 | (PARS_FORCE_GENERIC if force_generic else 0))
+        r = _lib.DeviceResult()
+        check(lib().pars_scan_device(self.ctx.handle, self.plan_id, ctypes.c_void_p(d_ptr), n,
+                                     flags, ctypes.c_void_p(stream), ctypes.byref(r)),
+              self.ctx.handle)
+        return DeviceResult(r, n)
+
+    def scan_tensor(self, t, **kw) -> DeviceResult:
+        """scan_device on a contiguous uint8 CUDA tensor."""
+        import torch
+        assert t.dtype == torch.uint8 and t.is_cuda and t.is_contiguous()
+        stream = kw.pop("stream", torch.cuda.current_stream().cuda_stream)
+        return self.scan_device(t.data_ptr(), t.numel(), stream=stream, **kw)
+
+    def scan_host(self, data, stream: int = 0, want_pairs: bool = False,
+                  want_chars: bool = False) -> HostResult:
+        a = np.ascontiguousarray(np.frombuffer(memoryview(data), np.uint8)
+                                 if not isinstance(data, np.ndarray) else data, dtype=np.uint8)
+        flags = PARS_RUN_PAIRS | (PARS_WANT_PAIRS if want_pairs else 0) | (
+            PARS_WANT_CHARS if want_chars else 0)
+        r = _lib.HostResult()
+        ptr = a.ctypes.data if a.size else None
+        check(lib().pars_scan_host(self.ctx.handle, self.plan_id, ctypes.c_void_p(ptr), a.size,
+                                   flags, ctypes.c_void_p(stream), ctypes.byref(r)),
+              self.ctx.handle)
+        n = int(r.n_struct)
+
+        def host(ptr, ct, dt):
+            if not ptr or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), (n,)).astype(dt)
+        return HostResult(host(r.structural, ctypes.c_uint32, np.uint32),
+                          host(r.pair_pos, ctypes.c_int32, np.int32),
+                          host(r.chars, ctypes.c_uint8, np.uint8),
+                          bool(r.balanced), bool(r.well_formed), int(r.max_depth),
+                          bool(r.unclosed_mode))
+
+    # ---- chunked stage 1 -----------------------------------------------------------
+    def reserve_struct(self, cap: int) -> None:
+        check(lib().pars_reserve_struct(self.ctx.handle, cap), self.ctx.handle)
+
+    def new_carry(self) -> _lib.ChunkCarry:
+        return _lib.ChunkCarry()
+
+    def scan_chunk(self, d_ptr: int, n: int, carry: _lib.ChunkCarry, stream: int = 0) -> None:
+        check(lib().pars_scan_chunk(self.ctx.handle, self.plan_id, ctypes.c_void_p(d_ptr), n,
+                                    ctypes.byref(carry), ctypes.c_void_p(stream)),
+              self.ctx.handle)
+
+    def chunk_finish(self, carry: _lib.ChunkCarry, stream: int = 0, want_pairs: bool = True,
+                     run_pairs: bool = True) -> DeviceResult:
+        flags = (PARS_WANT_PAIRS if want_pairs else 0) | (PARS_RUN_PAIRS if run_pairs else 0) \
+            | PARS_WANT_CHARS
+        r = _lib.DeviceResult()
+        check(lib().pars_chunk_finish(self.ctx.handle, self.plan_id, ctypes.byref(carry), flags,
+                                      ctypes.c_void_p(stream), ctypes.byref(r)), self.ctx.handle)
+        return DeviceResult(r, int(carry.byte_base))

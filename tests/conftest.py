@@ -1,0 +1,35 @@
+"""Shared fixtures.  GPU tests carry ``@pytest.mark.gpu``; everything else runs on CPU."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+GRAMMARS = ("json", "csv", "toml", "clike", "ini", "xml")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def plan_bytes(grammar: str) -> bytes:
+    with open(os.path.join(GOLDEN, "plans", f"{grammar}.plan"), "rb") as f:
+        return f.read()
+
+
+def golden_cases(grammar: str):
+    """Yield (name, case-dict) for every golden case of a grammar."""
+    z = np.load(os.path.join(GOLDEN, f"{grammar}.npz"))
+    for name in z["_cases"].tolist():
+        yield name, {k: z[f"{name}.{k}"] for k in
+                     ("in", "pos", "chars", "bpos", "bchar", "pair", "depth", "mask", "meta")}
+
+
+@pytest.fixture(scope="session")
+def plans():
+    return {g: plan_bytes(g) for g in GRAMMARS}

@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path against the golden fixtures (made by the unmodified
+reference CPU backend) and against the CPU oracle, bit-exact for every output:
+structural offsets, chars, bracket offsets/chars, depth keys, pairs (bracket and
+structural index space), per-byte masks, and the balanced / well_formed /
+max_depth / unclosed_mode flags."""
+import numpy as np
+import pytest
+
+from conftest import GRAMMARS, golden_cases, plan_bytes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle  # noqa: E402
+from pars_gb300 import Context, Scanner, synth  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return Context(0)
+
+
+@pytest.fixture(scope="module")
+def scanners(ctx):
+    return {g: Scanner(plan_bytes(g), ctx=ctx) for g in GRAMMARS}
+
+
+def to_dev(data: np.ndarray, offset: int = 0):
+    """Copy to the device at `offset` bytes past a 256-byte aligned allocation."""
+    buf = torch.zeros(data.size + offset + 64, dtype=torch.uint8, device="cuda")
+    if data.size:
+        buf[offset:offset + data.size] = torch.from_numpy(np.ascontiguousarray(data)).cuda()
+    return buf, buf.data_ptr() + offset
+
+
+def expected_from_oracle(plan, data):
+    sr = oracle.scan(plan, data)
+    pr = oracle.pair(plan, sr.bracket_char)
+    return {
+        "pos": sr.positions, "chars": sr.chars, "bpos": sr.bracket_pos, "bchar": sr.bracket_char,
+        "bpair": pr.pair, "depth": pr.depth, "mask": sr.mask,
+        "pair": oracle.pair_struct_space(sr, pr),
+        "meta": (sr.unclosed_mode, pr.balanced, pr.well_formed, pr.max_depth),
+    }
+
+
+def run(sc, data, offset=0, **kw):
+    buf, ptr = to_dev(data, offset)
+    want_mask = offset % 16 == 0
+    r = sc.scan_device(ptr, data.size, want_pairs=True, want_chars=True, want_mask=want_mask, **kw)
+    torch.cuda.synchronize()
+    g = r.to_numpy()
+    g["meta"] = (r.unclosed_mode, r.balanced, r.well_formed, r.max_depth)
+    g["path"] = r.kernel_path
+    del buf
+    return g
+
+
+def compare(g, e, name, mask=True):
+    for k in ("pos", "chars", "bpos", "bchar", "depth", "bpair", "pair"):
+        assert np.array_equal(g[k], e[k]), f"{name}: {k} differs"
+    if mask:
+        assert np.array_equal(g["mask"], e["mask"]), f"{name}: mask differs"
+    assert tuple(g["meta"]) == tuple(e["meta"]), f"{name}: flags {g['meta']} != {e['meta']}"
+
+
+@pytest.mark.parametrize("grammar", GRAMMARS)
+@pytest.mark.parametrize("generic", [False, True])
+def test_goldens(scanners, grammar, generic):
+    sc = scanners[grammar]
+    plan = plan_bytes(grammar)
+    for name, c in golden_cases(grammar):
+        g = run(sc, c["in"], force_generic=generic)
+        sr_pos = c["pos"]
+        e = {"pos": sr_pos, "chars": c["chars"], "bpos": c["bpos"], "bchar": c["bchar"],
+             "bpair": c["pair"], "depth": c["depth"], "mask": c["mask"],
+             "meta": tuple(bool(x) if i < 3 else int(x) for i, x in enumerate(
+                 [c["meta"][0], c["meta"][1], c["meta"][2], c["meta"][3]]))}
+        bsi = np.searchsorted(sr_pos, c["bpos"]).astype(np.int64)
+        ps = np.full(sr_pos.size, -1, np.int32)
+        has = c["pair"] >= 0
+        ps[bsi[has]] = bsi[c["pair"][has]]
+        e["pair"] = ps
+        compare(g, e, f"{grammar}/{name}/generic={generic}")
+
+
+def test_paths(scanners):
+    assert scanners["json"].path == "escape"
+    assert scanners["csv"].path == "doubled"
+    assert scanners["clike"].path == "generic"
+
+
+@pytest.mark.parametrize("grammar", GRAMMARS)
+@pytest.mark.parametrize("n", [1, 31, 33, 16383, 16385, 1 << 20, (3 << 20) + 7])
+def test_random_alphabet_vs_oracle(scanners, grammar, n):
+    from tests_alphabets import ALPHABETS
+    plan = plan_bytes(grammar)
+    data = synth.alpha(n * 31 + 7, ALPHABETS[grammar], n)
+    e = expected_from_oracle(plan, data)
+    compare(run(scanners[grammar], data), e, f"{grammar}/{n}")
+
+
+@pytest.mark.parametrize("offset", [1, 3, 8, 15])
+def test_unaligned_input(scanners, offset):
+    for g in ("json", "csv", "toml"):
+        data = synth.json_doc(offset, 200_000) if g == "json" else synth.csv_doc(offset, 200_000)
+        plan = plan_bytes(g)
+        e = expected_from_oracle(plan, data)
+        compare(run(scanners[g], data, offset=offset), e, f"{g}/off{offset}", mask=False)
+
+
+def test_json_64mib_config(scanners):
+    """The single-document JSON workload at its full 64 MiB size."""
+    plan = plan_bytes("json")
+    data = synth.json_doc(1, 64 << 20)
+    e = expected_from_oracle(plan, data)
+    g = run(scanners["json"], data)
+    compare(g, e, "json64")
+    assert g["path"] == "escape"
+
+
+def test_csv_full_size_properties(scanners):
+    """1 GiB CSV: size-independent properties, and exact equality with the oracle."""
+    plan = plan_bytes("csv")
+    data = synth.csv_doc(11, 1 << 30)
+    g = run(scanners["csv"], data)
+    pos = g["pos"]
+    assert np.all(np.diff(pos.astype(np.int64)) > 0)
+    assert np.all(np.isin(data[pos], np.frombuffer(b",\n", np.uint8)))
+    e = expected_from_oracle(plan, data)
+    compare(g, e, "csv1g")
+
+
+def test_scan_host_matches_device(scanners):
+    sc = scanners["json"]
+    data = synth.json_doc(5, 3 << 20)
+    h = sc.scan_host(data, want_pairs=True)
+    e = expected_from_oracle(plan_bytes("json"), data)
+    assert np.array_equal(h.structural, e["pos"])
+    assert np.array_equal(h.pair_pos, e["pair"])
+    assert (h.unclosed_mode, h.balanced, h.well_formed, h.max_depth) == e["meta"]
+
+
+@pytest.mark.parametrize("grammar", ["json", "csv", "toml", "xml"])
+def test_chunked_equals_whole(ctx, grammar):
+    plan = plan_bytes(grammar)
+    data = synth.json_doc(17, 3 << 20) if grammar == "json" else synth.csv_doc(17, 3 << 20) \
+        if grammar == "csv" else np.frombuffer(
+            (open(__file__, "rb").read() * 200)[:3 << 20], np.uint8).copy()
+    sc = Scanner(plan, ctx=ctx)
+    e = expected_from_oracle(plan, data)
+    buf, ptr = to_dev(data)
+    sc.reserve_struct(data.size + 1024)
+    carry = sc.new_carry()
+    cut = [0, 12345, 777777, 1 << 20, (2 << 20) + 3, data.size]
+    for a, b in zip(cut[:-1], cut[1:]):
+        sc.scan_chunk(ptr + a, b - a, carry)
+    r = sc.chunk_finish(carry)
+    torch.cuda.synchronize()
+    g = r.to_numpy()
+    assert np.array_equal(g["pos"], e["pos"])
+    assert np.array_equal(g["bpos"], e["bpos"])
+    assert np.array_equal(g["depth"], e["depth"])
+    assert np.array_equal(g["bpair"], e["bpair"])
+    assert (r.unclosed_mode, r.balanced, r.well_formed, r.max_depth) == e["meta"]
+
+
+def test_empty(scanners):
+    r = scanners["json"].scan_device(0, 0, want_pairs=True)
+    assert r.n_struct == 0 and r.balanced and r.well_formed and r.max_depth == 0
