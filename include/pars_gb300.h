@@ -161,6 +161,15 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
                       uint32_t flags, void* stream, pars_device_result* out);
 
+/* ---- profiling ------------------------------------------------------------ */
+/* cf. stage_times (pipeline.cuh:746-748, 767-774, 998-1011): when enabled, the
+ * context brackets its own launches with CUDA events on the caller's stream;
+ * pars_stage_times returns the last call's R1-R5 scan and R6 pairing times (ms).
+ * pars_launch_count returns how many kernels this context has launched. */
+int pars_set_profiling(pars_ctx* ctx, int enable);
+int pars_stage_times(pars_ctx* ctx, float* scan_ms, float* pairs_ms);
+uint64_t pars_launch_count(const pars_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

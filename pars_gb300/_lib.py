@@ -80,6 +80,10 @@ SIGNATURES = {
     "pars_chunk_finish": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ChunkCarry),
                                          ctypes.c_uint32, ctypes.c_void_p,
                                          ctypes.POINTER(DeviceResult)]),
+    "pars_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pars_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_float)]),
+    "pars_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
 }
 
 _LIB = None

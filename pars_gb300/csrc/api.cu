@@ -24,9 +24,11 @@
 
 namespace pars {
 
-// kernels (scan.cu / pair.cu)
+// kernels (scan_fast.cu / scan.cu / pair.cu)
 int		   scan_smem_bytes(int path);
 const void* scan_kernel(int path);
+int		   scan_fast_smem_bytes();
+const void* scan_fast_kernel(int path, bool brackets);
 int		   sort_tile_keys();
 struct SortPass;
 __global__ void k_sort_pass(const SortPass p);
@@ -78,6 +80,7 @@ struct pars_ctx {
 	uint64_t		   arena_used  = 0;
 	int				   num_sms	   = 0;
 	int				   scan_blocks[5] = {0, 0, 0, 0, 0};
+	int				   fast_blocks[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	std::string		   err;
 	std::vector<Plan*> plans;
 	unsigned int	   epoch = 0;
@@ -85,6 +88,7 @@ struct pars_ctx {
 	// scratch
 	DevBuf tiles, lb, sort_keys_a, sort_keys_b, sort_idx_b, digit_hist;
 	Counters*  ctr		= nullptr;
+	ResBlock*  rb		= nullptr;	// result block + key histogram (one allocation)
 	DevResult* res		= nullptr;
 	unsigned int* key_hist = nullptr;
 	DevCarry*  carry	= nullptr;	// [2] ping-pong for chunks
@@ -103,6 +107,11 @@ struct pars_ctx {
 	// chunk state
 	uint64_t chunk_index = 0;
 	cudaEvent_t ev = nullptr;
+	// profiling
+	bool		profiling = false;
+	cudaEvent_t prof[3] = {nullptr, nullptr, nullptr};
+	bool		prof_pairs = false;
+	uint64_t	launches   = 0;
 };
 
 namespace {
@@ -148,7 +157,13 @@ int grow(pars_ctx* ctx, DevBuf& b, size_t bytes) {
 	cudaError_t e = cudaMalloc(&b.p, want);
 	if (e != cudaSuccess) {
 		cudaGetLastError();
-		return cuda_fail(ctx, e, "cudaMalloc");
+		size_t fr = 0, tot = 0;
+		cudaMemGetInfo(&fr, &tot);
+		char msg[160];
+		std::snprintf(msg, sizeof msg, "cudaMalloc(%zu) [free %zu MiB of %zu MiB, ctx holds %llu MiB]",
+					  want, fr >> 20, tot >> 20,
+					  static_cast<unsigned long long>(ctx->arena_used >> 20));
+		return cuda_fail(ctx, e, msg);
 	}
 	b.cap = want;
 	ctx->arena_used += want;
@@ -320,16 +335,41 @@ struct Scan {
 	DevCarry*	   carry_out;
 };
 
-int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s) {
+int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
+	const int slot = path * 2 + (br ? 1 : 0);
+	if (ctx->fast_blocks[slot])
+		return 0;
+	const void* k	 = scan_fast_kernel(path, br);
+	const int	smem = scan_fast_smem_bytes();
+	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	int per_sm = 0;
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kScanThreads, smem));
+	if (per_sm < 1)
+		return fail(ctx, PARS_ECUDA, "fast scan kernel does not fit on an SM");
+	// the look-back window of a tile spans one wave (G tiles): keep G <= 512
+	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, 512);
+	return 0;
+}
+
+// `first` = first launch of a document: clears the result block + key histogram.
+int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true) {
 	const uint64_t o	 = reinterpret_cast<uintptr_t>(s.d_in) & 15u;
 	const uint8_t* base	 = s.d_in - o;
 	const uint64_t total = o + s.n;
 	const uint64_t ntiles = (total + kTileBytes - 1) / kTileBytes;
-	const size_t tdesc = s.path == kPathGeneric ? sizeof(TileDescG) : sizeof(TileDesc);
+	const bool	   fast	 = s.path != kPathGeneric;
+	const size_t tdesc = fast ? sizeof(uint4) : sizeof(TileDescG);
 	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
 		return r;
-	if (int r = ensure_scan_config(ctx, s.path))
-		return r;
+	if (fast) {
+		if (int r = ensure_fast_config(ctx, s.path, pl->host.has_brackets != 0))
+			return r;
+	} else {
+		if (int r = ensure_scan_config(ctx, s.path))
+			return r;
+	}
+	if (first)
+		CK(cudaMemsetAsync(ctx->rb, 0, sizeof(ResBlock), s.st));
 	ScanArgs a {};
 	a.base		= base;
 	a.o			= o;
@@ -355,10 +395,18 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s) {
 	a.carry_out = s.carry_out;
 	a.epoch		= next_epoch(ctx);
 	a.flags		= s.flags;
-	const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
-	void*	  args[] = {&a};
-	CK(cudaLaunchKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,
-						scan_smem_bytes(s.path), s.st));
+	void* args[] = {&a};
+	if (fast) {
+		const bool br	= pl->host.has_brackets != 0;
+		const int  grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
+		CK(cudaLaunchCooperativeKernel(scan_fast_kernel(s.path, br), dim3(grid), dim3(kScanThreads),
+									   args, scan_fast_smem_bytes(), s.st));
+	} else {
+		const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
+		CK(cudaLaunchCooperativeKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,
+									   scan_smem_bytes(s.path), s.st));
+	}
+	ctx->launches++;
 	return 0;
 }
 
@@ -398,11 +446,13 @@ int launch_pairs_speculative(pars_ctx* ctx, const Plan* pl, uint32_t flags, cuda
 	void*	  a1[] = {&sp};
 	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(grid), dim3(256), a1, 0,
 						st));
+	ctx->launches++;
 	PairArgs pa	  = pair_args(ctx, pl, flags, static_cast<const uint32_t*>(ctx->order.p));
 	int		 req  = 1;
 	void*	 a2[] = {&pa, &req};
 	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pair), dim3(ctx->num_sms * 4), dim3(256), a2,
 						0, st));
+	ctx->launches++;
 	return 0;
 }
 
@@ -410,7 +460,7 @@ int launch_pairs_speculative(pars_ctx* ctx, const Plan* pl, uint32_t flags, cuda
 int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t st,
 				   const DevResult& r) {
 	const uint64_t n = r.n_brackets;
-	const uint64_t range = static_cast<uint64_t>(r.max_key - r.min_key) + 1;
+	const uint64_t range = static_cast<uint64_t>(dec_max(r.max_key) - dec_min(r.min_key)) + 1;
 	int passes = 1;
 	while (passes < 4 && (range >> (8 * passes)) > 0) ++passes;
 	const uint64_t ntiles_sort = (n + sort_tile_keys() - 1) / sort_tile_keys() + 1;
@@ -435,6 +485,7 @@ int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t s
 		k_digit_hist<<<ctx->num_sms * 4, 256, 0, st>>>(kin, ctx->res, 8u * ps,
 													   static_cast<unsigned int*>(ctx->digit_hist.p));
 		CK(cudaGetLastError());
+		ctx->launches++;
 		SortPass sp {};
 		sp.keys_in	  = kin;
 		sp.idx_in	  = iin;
@@ -452,6 +503,7 @@ int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t s
 		void* a1[]	  = {&sp};
 		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4),
 							dim3(256), a1, 0, st));
+		ctx->launches++;
 		kin = kbuf[out];
 		iin = ibuf[out];
 		out ^= 1;
@@ -461,6 +513,7 @@ int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t s
 	void*	 a2[] = {&pa, &req};
 	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pair), dim3(ctx->num_sms * 4), dim3(256), a2,
 						0, st));
+	ctx->launches++;
 	return 0;
 }
 
@@ -507,7 +560,7 @@ int ensure_outputs(pars_ctx* ctx, uint64_t cap_s, uint64_t cap_b, uint64_t n, ui
 int reset_after_error(pars_ctx* ctx, cudaStream_t st) {
 	CK(cudaStreamSynchronize(st));
 	CK(cudaMemset(ctx->ctr, 0, sizeof(Counters)));
-	CK(cudaMemset(ctx->res, 0, sizeof(DevResult)));
+	CK(cudaMemset(ctx->rb, 0, sizeof(ResBlock)));
 	if (ctx->tiles.p)
 		CK(cudaMemset(ctx->tiles.p, 0, ctx->tiles.cap));
 	if (ctx->lb.p)
@@ -520,7 +573,7 @@ void fill_result(pars_ctx* ctx, const DevResult& r, uint32_t flags, bool pairs_r
 	std::memset(out, 0, sizeof *out);
 	out->structural	  = static_cast<const uint32_t*>(ctx->pos.p);
 	out->chars		  = (flags & PARS_WANT_CHARS) ? static_cast<const uint8_t*>(ctx->chars.p) : nullptr;
-	out->pair_pos	  = (flags & PARS_WANT_PAIRS) && pairs_ran ? static_cast<const int32_t*>(ctx->pair.p) : nullptr;
+	out->pair_pos	  = (flags & PARS_WANT_PAIRS) ? static_cast<const int32_t*>(ctx->pair.p) : nullptr;
 	out->bracket_pos  = static_cast<const uint32_t*>(ctx->bpos.p);
 	out->bracket_char = static_cast<const uint8_t*>(ctx->bchar.p);
 	out->bracket_struct = static_cast<const uint32_t*>(ctx->bsi.p);
@@ -572,11 +625,18 @@ int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, u
 		if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
 			return r;
 		Scan s {d_in, n, flags, st, path, nullptr, nullptr};
+		if (ctx->profiling)
+			CK(cudaEventRecord(ctx->prof[0], st));
 		if (int r = launch_scan(ctx, pl, s))
 			return r;
+		if (ctx->profiling)
+			CK(cudaEventRecord(ctx->prof[1], st));
 		if (run_pairs)
 			if (int r = launch_pairs_speculative(ctx, pl, flags, st))
 				return r;
+		if (ctx->profiling)
+			CK(cudaEventRecord(ctx->prof[2], st));
+		ctx->prof_pairs = run_pairs;
 		CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
 		CK(cudaStreamSynchronize(st));
 		DevResult r = *ctx->h_res;
@@ -650,11 +710,12 @@ int pars_create(int device, uint64_t arena_bytes, pars_ctx** out) {
 		return err == cudaErrorMemoryAllocation ? PARS_ENOMEM : PARS_ECUDA;
 	};
 	if ((e = cudaMalloc(&ctx->ctr, sizeof(Counters))) != cudaSuccess) return bail(e);
-	if ((e = cudaMalloc(&ctx->res, sizeof(DevResult))) != cudaSuccess) return bail(e);
-	if ((e = cudaMalloc(&ctx->key_hist, 2 * kKeyWindow * sizeof(unsigned int))) != cudaSuccess) return bail(e);
+	if ((e = cudaMalloc(&ctx->rb, sizeof(ResBlock))) != cudaSuccess) return bail(e);
+	ctx->res	  = &ctx->rb->r;
+	ctx->key_hist = ctx->rb->key_hist;
 	if ((e = cudaMalloc(&ctx->carry, 2 * sizeof(DevCarry))) != cudaSuccess) return bail(e);
 	if ((e = cudaMemset(ctx->ctr, 0, sizeof(Counters))) != cudaSuccess) return bail(e);
-	if ((e = cudaMemset(ctx->res, 0, sizeof(DevResult))) != cudaSuccess) return bail(e);
+	if ((e = cudaMemset(ctx->rb, 0, sizeof(ResBlock))) != cudaSuccess) return bail(e);
 	if ((e = cudaMemset(ctx->carry, 0, 2 * sizeof(DevCarry))) != cudaSuccess) return bail(e);
 	if ((e = cudaHostAlloc(&ctx->h_res, sizeof(DevResult), cudaHostAllocDefault)) != cudaSuccess)
 		return bail(e);
@@ -674,8 +735,7 @@ int pars_destroy(pars_ctx* ctx) {
 		if (b->p)
 			cudaFree(b->p);
 	if (ctx->ctr) cudaFree(ctx->ctr);
-	if (ctx->res) cudaFree(ctx->res);
-	if (ctx->key_hist) cudaFree(ctx->key_hist);
+	if (ctx->rb) cudaFree(ctx->rb);
 	if (ctx->carry) cudaFree(ctx->carry);
 	if (ctx->h_res) cudaFreeHost(ctx->h_res);
 	if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -683,6 +743,9 @@ int pars_destroy(pars_ctx* ctx) {
 	if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
 	if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
 	if (ctx->ev) cudaEventDestroy(ctx->ev);
+	for (cudaEvent_t& e : ctx->prof)
+		if (e)
+			cudaEventDestroy(e);
 	for (Plan* p : ctx->plans) {
 		if (p->dev)
 			cudaFree(p->dev);
@@ -839,7 +902,7 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 	DevCarry* cin  = ctx->carry + (ctx->chunk_index & 1);
 	DevCarry* cout = ctx->carry + ((ctx->chunk_index + 1) & 1);
 	Scan s {d_chunk, n, PARS_WANT_PAIRS | PARS_WANT_CHARS, st, path, cin, cout};
-	if (int r = launch_scan(ctx, pl, s))
+	if (int r = launch_scan(ctx, pl, s, ctx->chunk_index == 0))
 		return r;
 	ctx->chunk_index++;
 	carry->byte_base += n;
@@ -892,6 +955,34 @@ int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
 	}
 	fill_result(ctx, r, flags, run_pairs, out);
 	return 0;
+}
+
+int pars_set_profiling(pars_ctx* ctx, int enable) {
+	if (!ctx)
+		return PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	if (enable && !ctx->prof[0])
+		for (cudaEvent_t& e : ctx->prof) CK(cudaEventCreate(&e));
+	ctx->profiling = enable != 0;
+	return 0;
+}
+
+int pars_stage_times(pars_ctx* ctx, float* scan_ms, float* pairs_ms) {
+	if (!ctx || !ctx->profiling)
+		return PARS_EINVAL;
+	float a = 0, b = 0;
+	CK(cudaEventSynchronize(ctx->prof[2]));
+	CK(cudaEventElapsedTime(&a, ctx->prof[0], ctx->prof[1]));
+	CK(cudaEventElapsedTime(&b, ctx->prof[1], ctx->prof[2]));
+	if (scan_ms)
+		*scan_ms = a;
+	if (pairs_ms)
+		*pairs_ms = ctx->prof_pairs ? b : 0.0f;
+	return 0;
+}
+
+uint64_t pars_launch_count(const pars_ctx* ctx) {
+	return ctx ? ctx->launches : 0;
 }
 
 }  // extern "C"

@@ -68,13 +68,13 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(const SortPass p) {
 	DevResult* res = p.res;
 	const int  tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const unsigned long long n = res->n_brackets;
-	const long long			 kmin = res->min_key;
+	const long long			 kmin = n ? dec_min(res->min_key) : 0;
 
 	if (p.first) {
 		// speculative single pass: only when every key sits in the window and the
 		// key range fits one 8-bit digit
 		const bool ok = !res->keys_oob && !res->error && n <= p.cap
-					 && (n == 0 || res->max_key - kmin < 256);
+					 && (n == 0 || dec_max(res->max_key) - kmin < 256);
 		if (blockIdx.x == 0 && tid == 0)
 			res->sort_ok = ok ? 1u : 0u;
 		if (!ok || n == 0)
@@ -219,7 +219,7 @@ __global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, uns
 	h[threadIdx.x] = 0;
 	__syncthreads();
 	const unsigned long long n	  = res->n_brackets;
-	const long long			 kmin = res->min_key;
+	const long long			 kmin = n ? dec_min(res->min_key) : 0;
 	for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += gridDim.x * 256ull) {
 		const std::uint32_t d =
 			static_cast<std::uint32_t>(static_cast<unsigned long long>(keys[i] - kmin) >> shift)
@@ -291,11 +291,13 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort
 		if (done == gridDim.x - 1) {
 			__threadfence();
 			const long long	 fin = static_cast<long long>(res->n_open) - static_cast<long long>(res->n_close);
-			const bool		 bal = res->min_bal >= 0 && fin == 0;
+			const long long	 mnb = res->min_bal ? dec_min(res->min_bal) : 0;
+			const long long	 mxb = res->max_bal ? dec_max(res->max_bal) : 0;
+			const bool		 bal = mnb >= 0 && fin == 0;
 			const unsigned int mis = *reinterpret_cast<volatile unsigned int*>(&res->mismatch);
 			res->balanced		 = bal ? 1u : 0u;
 			res->well_formed	 = (bal && !mis && (n % 2 == 0)) ? 1u : 0u;
-			res->max_depth		 = static_cast<int>(res->max_bal > 0 ? res->max_bal : 0);
+			res->max_depth		 = static_cast<int>(mxb > 0 ? mxb : 0);
 			a.ctr->pair_done	 = 0;
 			__threadfence();
 		}

@@ -49,16 +49,38 @@ struct DevPlan {
 	std::uint8_t  pad0;
 };
 
-// Per-scan result block written by the kernels and read back by the host.
+// Depth extrema are kept in zero-initialised unsigned fields so that a plain
+// memset resets them: 0 means "no bracket seen"; otherwise
+//   min field = kMinBase - (v + kBias)   (maximised with atomicMax)
+//   max field = v + kBias + 1            (maximised with atomicMax)
+constexpr long long			 kExtBias = 1ll << 40;
+constexpr unsigned long long kMinBase = 1ull << 62;
+
+__host__ __device__ inline unsigned long long enc_min(long long v) {
+	return kMinBase - static_cast<unsigned long long>(v + kExtBias);
+}
+__host__ __device__ inline unsigned long long enc_max(long long v) {
+	return static_cast<unsigned long long>(v + kExtBias) + 1ull;
+}
+__host__ __device__ inline long long dec_min(unsigned long long f) {
+	return static_cast<long long>(kMinBase - f) - kExtBias;
+}
+__host__ __device__ inline long long dec_max(unsigned long long f) {
+	return static_cast<long long>(f - 1ull) - kExtBias;
+}
+
+// Per-scan result block written by the kernels and read back by the host.  The
+// host clears it (one memset with the key histogram that follows it) before a
+// document's first scan launch.
 struct DevResult {
 	unsigned long long n_struct;
 	unsigned long long n_brackets;
 	unsigned long long n_open;
 	unsigned long long n_close;
-	long long		   min_bal;	   // min over brackets of the running depth (init 0)
-	long long		   max_bal;	   // max over brackets of the running depth (init 0)
-	long long		   min_key;
-	long long		   max_key;
+	unsigned long long min_bal;	   // encoded (enc_min), 0 = none
+	unsigned long long max_bal;	   // encoded (enc_max), 0 = none
+	unsigned long long min_key;	   // encoded (enc_min), 0 = none
+	unsigned long long max_key;	   // encoded (enc_max), 0 = none
 	unsigned int	   unclosed;
 	unsigned int	   spec_fail;	// escape path: a quote escaped outside a string
 	unsigned int	   keys_oob;	// a depth key fell outside [-1024, 1024)
@@ -70,6 +92,13 @@ struct DevResult {
 	int				   max_depth;
 	unsigned int	   path;
 	unsigned int	   pad[2];
+};
+
+// The result block and the 2048-bin key histogram live in one allocation so one
+// memset clears both.
+struct ResBlock {
+	DevResult	 r;
+	unsigned int key_hist[2048];
 };
 
 // State at a chunk boundary (device resident; chained chunk to chunk).

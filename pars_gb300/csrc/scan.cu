@@ -359,24 +359,6 @@ struct SmemLayout {
 	static constexpr int kBytesGen	= kGen + 8 * 256 + 8 * 64 + 2 * 8 * 8 * 4;
 };
 
-// First tile of a scan initialises the result block (and, for the first chunk of
-// a document, the running depth extrema and key histogram) before it publishes,
-// so every other tile's atomics on them happen after.
-__device__ __forceinline__ void init_result(DevResult* res, int path, bool first_chunk) {
-	if (first_chunk) {
-		res->min_bal = 0;
-		res->max_bal = 0;
-		res->min_key = 0x7FFFFFFFFFFFFFFFll;
-		res->max_key = -0x7FFFFFFFFFFFFFFFll;
-		res->keys_oob = 0;
-	}
-	res->unclosed  = 0;
-	res->spec_fail = 0;
-	res->mismatch  = 0;
-	res->sort_ok   = 0;
-	res->path	   = path;
-}
-
 }  // namespace
 
 // ============================================================================
@@ -423,8 +405,11 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 	__syncthreads();
 
 	std::uint32_t pending = 0;	// tid 0: stages with a bulk copy in flight
-	auto issue = [&](int s) {  // tid 0 only: take a ticket and start its copy
-		const unsigned long long t = atomicAdd(&a.ctr->scan_ticket, 1u);
+	// static schedule (cooperative launch): CTA b owns tiles b, b + G, b + 2G, ...
+	unsigned long long next_k = 0;
+	auto issue = [&](int s) {  // tid 0 only: start the copy of my next tile
+		const unsigned long long t = blockIdx.x + next_k * gridDim.x;
+		++next_k;
 		sc.tile_id[s]			   = t;
 		if (t < a.ntiles) {
 			pending |= 1u << s;
@@ -592,11 +577,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 					if (t == 0)
 						sc.init_state = a.carry_in ? a.carry_in->fstate : 0u;
 					tiles[t].inc1 = compose_fast(texcl, agg);
-					if (t == 0)
-						init_result(res, PATH, first_chunk);
+
 				}
-				if (t == 0 && brk && first_chunk)
-					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
 				__syncwarp();
 				if (lane == 0)
 					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
@@ -632,21 +614,15 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 						for (int d = 0; d < 8; ++d)
 							sc.init_gstate[d] = a.carry_in ? a.carry_in->gstate[d]
 														   : (d < nd ? P->start[d] : 0u);
-						init_result(res, PATH, first_chunk);
 					}
 				}
-				if (t == 0 && brk && first_chunk)
-					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
 				__syncwarp();
 				if (lane == 0)
 					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
 				if (lane < 16)
 					for (int d = 0; d < nd; ++d) sc.warp_maps[lane][d] = compose_map(texcl[d], we[d]);
 			} else {  // kPathNone: still publish so the structure is uniform
-				if (lane == 0 && t == 0)
-					init_result(res, PATH, first_chunk);
-				if (t == 0 && brk && first_chunk)
-					for (int i = lane; i < 2 * kKeyWindow; i += 32) a.key_hist[i] = 0;
+
 			}
 			if (fail && lane == 0)
 				sc.failed = 1;
@@ -813,6 +789,7 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 				if (fail)
 					sc.failed = 1;
 				if (t == a.ntiles - 1) {
+					res->path		= PATH;
 					res->n_struct	= base[0] + tot[0];
 					res->n_open		= base[1] + tot[1];
 					res->n_close	= base[2] + tot[2];
@@ -873,6 +850,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 					a.pos[si] = pos;
 					if (want_chars)
 						a.chars[si] = wb[j];
+					if (want_pairs)
+						a.pair[si] = -1;  // bracket entries are overwritten by R6
 				}
 				if ((bm >> j) & 1u) {
 					const bool op  = (selo >> j) & 1u;
@@ -894,8 +873,6 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 						atomicAdd(&khist[key + kKeyWindow], 1u);
 					else
 						atomicOr(&res->keys_oob, 1u);
-				} else if (want_pairs && si < a.cap_s) {
-					a.pair[si] = -1;
 				}
 				++si;
 			}
@@ -949,33 +926,18 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
 				kn = sc.wmin_key[w] < kn ? sc.wmin_key[w] : kn;
 				kx = sc.wmax_key[w] > kx ? sc.wmax_key[w] : kx;
 			}
-			atomicMin(&res->min_bal, mn);
-			atomicMax(&res->max_bal, mx);
-			atomicMin(&res->min_key, kn);
-			atomicMax(&res->max_key, kx);
+			atomicMax(&res->min_bal, enc_min(mn));
+			atomicMax(&res->max_bal, enc_max(mx));
+			atomicMax(&res->min_key, enc_min(kn));
+			atomicMax(&res->max_key, enc_max(kx));
 		}
 		if (sc.any_br && !sc.failed)
 			for (int i = tid; i < 2 * kKeyWindow; i += kScanThreads)
 				if (khist[i])
 					atomicAdd(&a.key_hist[i], khist[i]);
 	}
-	// ---- last CTA out resets the tickets for the next launch ------------------------
-	__syncthreads();
-	if (tid == 0) {
-		__threadfence();
-		const unsigned int done = atomicAdd(&a.ctr->scan_done, 1u);
-		if (done == gridDim.x - 1) {
-			a.ctr->scan_ticket = 0;
-			a.ctr->scan_done   = 0;
-			__threadfence();
-		}
-	}
 }
 
-template __global__ void k_scan<kPathNone>(const ScanArgs);
-template __global__ void k_scan<kPathParity>(const ScanArgs);
-template __global__ void k_scan<kPathDoubled>(const ScanArgs);
-template __global__ void k_scan<kPathEscape>(const ScanArgs);
 template __global__ void k_scan<kPathGeneric>(const ScanArgs);
 
 int scan_smem_bytes(int path) {
@@ -983,13 +945,8 @@ int scan_smem_bytes(int path) {
 }
 
 const void* scan_kernel(int path) {
-	switch (path) {
-		case kPathNone: return reinterpret_cast<const void*>(&k_scan<kPathNone>);
-		case kPathParity: return reinterpret_cast<const void*>(&k_scan<kPathParity>);
-		case kPathDoubled: return reinterpret_cast<const void*>(&k_scan<kPathDoubled>);
-		case kPathEscape: return reinterpret_cast<const void*>(&k_scan<kPathEscape>);
-		default: return reinterpret_cast<const void*>(&k_scan<kPathGeneric>);
-	}
+	(void)path;
+	return reinterpret_cast<const void*>(&k_scan<kPathGeneric>);
 }
 
 }  // namespace pars

@@ -32,7 +32,7 @@ class _DevArray:
 
     def __init__(self, ptr: int, n: int, typestr: str):
         self.__cuda_array_interface__ = {
-            "shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), True),
+            "shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), False),
             "version": 2, "strides": None,
         }
 
