@@ -28,6 +28,7 @@ namespace pars {
 int		   scan_smem_bytes(int path);
 const void* scan_kernel(int path);
 int		   scan_fast_smem_bytes();
+int		   scan_fast_max_grid();
 const void* scan_fast_kernel(int path, bool brackets);
 int		   sort_tile_keys();
 struct SortPass;
@@ -138,7 +139,7 @@ int cuda_fail(pars_ctx* c, cudaError_t e, const char* what) {
 			return cuda_fail(ctx, e_, #call);           \
 	} while (0)
 
-int grow(pars_ctx* ctx, DevBuf& b, size_t bytes) {
+int grow_impl(pars_ctx* ctx, DevBuf& b, size_t bytes, const char* what) {
 	if (bytes <= b.cap)
 		return 0;
 	size_t want = std::max(bytes, b.cap + b.cap / 2);
@@ -159,9 +160,9 @@ int grow(pars_ctx* ctx, DevBuf& b, size_t bytes) {
 		cudaGetLastError();
 		size_t fr = 0, tot = 0;
 		cudaMemGetInfo(&fr, &tot);
-		char msg[160];
-		std::snprintf(msg, sizeof msg, "cudaMalloc(%zu) [free %zu MiB of %zu MiB, ctx holds %llu MiB]",
-					  want, fr >> 20, tot >> 20,
+		char msg[256];
+		std::snprintf(msg, sizeof msg, "cudaMalloc(%s, %zu) [free %zu MiB of %zu MiB, ctx holds %llu MiB]",
+					  what, want, fr >> 20, tot >> 20,
 					  static_cast<unsigned long long>(ctx->arena_used >> 20));
 		return cuda_fail(ctx, e, msg);
 	}
@@ -169,6 +170,8 @@ int grow(pars_ctx* ctx, DevBuf& b, size_t bytes) {
 	ctx->arena_used += want;
 	return 0;
 }
+
+#define grow(ctx, buf, bytes) grow_impl(ctx, buf, bytes, #buf)
 
 // ---- plan analysis -------------------------------------------------------------
 // Canonical automata of the fast paths, over byte roles X (other), Q (delimiter),
@@ -346,8 +349,8 @@ int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
 	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kScanThreads, smem));
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "fast scan kernel does not fit on an SM");
-	// the look-back window of a tile spans one wave (G tiles): keep G <= 512
-	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, 512);
+	// the look-back window of a tile spans one wave (G tiles), held by one warp
+	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, scan_fast_max_grid());
 	return 0;
 }
 
@@ -358,7 +361,7 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	const uint64_t total = o + s.n;
 	const uint64_t ntiles = (total + kTileBytes - 1) / kTileBytes;
 	const bool	   fast	 = s.path != kPathGeneric;
-	const size_t tdesc = fast ? sizeof(uint4) : sizeof(TileDescG);
+	const size_t tdesc = fast ? 2 * sizeof(uint4) : sizeof(TileDescG);  // fast: AGG + INCL words
 	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
 		return r;
 	if (fast) {
@@ -882,7 +885,7 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 	Plan* pl = get_plan(ctx, plan_id);
 	if (!pl || !carry || (n && !d_chunk))
 		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
-	if (carry->byte_base + n >= (1ull << 32))
+	if (n >= (1ull << 32) || carry->byte_base >= (1ull << 32) || carry->byte_base + n >= (1ull << 32))
 		return fail(ctx, PARS_ERANGE, "document larger than 2^32-1 bytes");
 	cudaSetDevice(ctx->device);
 	cudaStream_t st = static_cast<cudaStream_t>(stream);

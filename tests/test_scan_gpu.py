@@ -144,9 +144,14 @@ def test_scan_host_matches_device(scanners):
 @pytest.mark.parametrize("grammar", ["json", "csv", "toml", "xml"])
 def test_chunked_equals_whole(ctx, grammar):
     plan = plan_bytes(grammar)
-    data = synth.json_doc(17, 3 << 20) if grammar == "json" else synth.csv_doc(17, 3 << 20) \
-        if grammar == "csv" else np.frombuffer(
-            (open(__file__, "rb").read() * 200)[:3 << 20], np.uint8).copy()
+    if grammar == "json":
+        data = synth.json_doc(17, 3 << 20)
+    elif grammar == "csv":
+        data = synth.csv_doc(17, 3 << 20)
+    else:
+        src = open(__file__, "rb").read()
+        data = np.frombuffer((src * ((3 << 20) // len(src) + 1))[:3 << 20], np.uint8).copy()
+    assert data.size >= (2 << 20) + 4
     sc = Scanner(plan, ctx=ctx)
     e = expected_from_oracle(plan, data)
     buf, ptr = to_dev(data)
