@@ -29,6 +29,9 @@ int		   scan_smem_bytes(int path);
 const void* scan_kernel(int path);
 int		   scan_fast_smem_bytes();
 int		   scan_fast_max_grid();
+int		   scan_ws_threads();
+int		   scan_ws_smem_bytes();
+const void* scan_ws_kernel(int path, bool brackets);
 const void* scan_fast_kernel(int path, bool brackets);
 int		   sort_tile_keys();
 struct SortPass;
@@ -338,15 +341,33 @@ struct Scan {
 	DevCarry*	   carry_out;
 };
 
+// The parity / doubled / no-descriptor paths run the warp-specialised kernel
+// (scan_ws.cu); the escape path runs scan_fast.cu; everything else scan.cu.
+bool use_ws(int path) {
+	return path == kPathNone || path == kPathParity || path == kPathDoubled;
+}
+
+const void* fast_kernel(int path, bool br) {
+	return use_ws(path) ? scan_ws_kernel(path, br) : scan_fast_kernel(path, br);
+}
+
+int fast_threads(int path) {
+	return use_ws(path) ? scan_ws_threads() : kScanThreads;
+}
+
+int fast_smem(int path) {
+	return use_ws(path) ? scan_ws_smem_bytes() : scan_fast_smem_bytes();
+}
+
 int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
 	const int slot = path * 2 + (br ? 1 : 0);
 	if (ctx->fast_blocks[slot])
 		return 0;
-	const void* k	 = scan_fast_kernel(path, br);
-	const int	smem = scan_fast_smem_bytes();
+	const void* k	 = fast_kernel(path, br);
+	const int	smem = fast_smem(path);
 	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 	int per_sm = 0;
-	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kScanThreads, smem));
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, fast_threads(path), smem));
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "fast scan kernel does not fit on an SM");
 	// the look-back window of a tile spans one wave (G tiles), held by one warp
@@ -402,8 +423,8 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	if (fast) {
 		const bool br	= pl->host.has_brackets != 0;
 		const int  grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
-		CK(cudaLaunchCooperativeKernel(scan_fast_kernel(s.path, br), dim3(grid), dim3(kScanThreads),
-									   args, scan_fast_smem_bytes(), s.st));
+		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br), dim3(grid), dim3(fast_threads(s.path)),
+									   args, fast_smem(s.path), s.st));
 	} else {
 		const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
 		CK(cudaLaunchCooperativeKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,

@@ -1,0 +1,81 @@
+// fast_common.cuh — pieces shared by the fast scan kernels (scan_fast.cu, scan_ws.cu).
+#pragma once
+
+#include "scan_common.cuh"
+
+namespace pars {
+namespace scan_detail {
+
+constexpr std::uint32_t kDAgg  = 1u << 30;
+constexpr std::uint32_t kDIncl = 2u << 30;
+constexpr int			kRing  = 3;
+constexpr int			kLB	   = 5;	 // look-back words per lane of warp 0: G <= 32 * kLB
+
+__device__ __forceinline__ std::uint32_t half16(std::uint32_t x, std::uint32_t h) {
+	return h ? (x >> 16) : (x & 0xFFFFu);
+}
+
+// Counts of a tile (AGG payload) when it is entered in state s = (e, p).
+template<int PATH>
+__device__ __forceinline__ void agg_counts(const uint4& v, std::uint32_t s, std::uint32_t& cs,
+										   std::uint32_t& co, std::uint32_t& cc) {
+	if (PATH == kPathNone) {
+		cs = v.x;
+		co = v.y;
+		cc = v.z;
+		return;
+	}
+	const std::uint32_t e = s & 1u, p = (s >> 1) & 1u;
+	const std::uint32_t d	= (v.w >> 3) & 1u;
+	const std::uint32_t fcl = (v.w >> 4) & 7u;
+	const std::uint32_t h	= p ^ (e & d);
+	const std::uint32_t lo	= p ? 0u : 1u;
+	cs = half16(v.x, h) + ((fcl & 1u) ? lo : 0u);
+	co = half16(v.y, h) + ((fcl & 2u) ? lo : 0u);
+	cc = half16(v.z, h) + ((fcl & 4u) ? lo : 0u);
+}
+
+// lanes: [0] packed S counts (hyp 0 | hyp 1 << 16), [1] parity, [2] packed O, [3] packed C
+struct OpParity {
+	__device__ __forceinline__ void operator()(const std::uint32_t (&a)[4], std::uint32_t (&b)[4]) const {
+		const std::uint32_t sw = a[1] ? 0x1032u : 0x3210u;
+		b[0] = a[0] + __byte_perm(b[0], 0, sw);
+		b[1] ^= a[1];
+		b[2] = a[2] + __byte_perm(b[2], 0, sw);
+		b[3] = a[3] + __byte_perm(b[3], 0, sw);
+	}
+};
+
+// R1 for one 32-byte word.  r[0..3] hold half `sw`, r[4..7] the other half; the
+// final byte permutes put the two halves back in order.
+__device__ __forceinline__ void classify_word(const std::uint32_t (&r)[8], std::uint32_t tbl_lane,
+											  std::uint32_t selA, std::uint32_t selB,
+											  std::uint32_t& P0, std::uint32_t& P1,
+											  std::uint32_t& P2, std::uint32_t& P3) {
+	std::uint32_t acc[4];
+#pragma unroll
+	for (int g = 0; g < 4; ++g) {
+		std::uint32_t a = 0;
+#pragma unroll
+		for (int jj = 0; jj < 8; ++jj) {
+			const int			j	 = g * 8 + jj;
+			const std::uint32_t addr = __byte_perm(r[j >> 2], tbl_lane, 0x7604u | ((j & 3) << 4));
+			std::uint32_t		v;
+			asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+			a += v << jj;
+		}
+		acc[g] = a;
+	}
+	const std::uint32_t t0 = __byte_perm(acc[0], acc[1], 0x5140);
+	const std::uint32_t t1 = __byte_perm(acc[0], acc[1], 0x7362);
+	const std::uint32_t t2 = __byte_perm(acc[2], acc[3], 0x5140);
+	const std::uint32_t t3 = __byte_perm(acc[2], acc[3], 0x7362);
+	P0					   = __byte_perm(t0, t2, selA);
+	P1					   = __byte_perm(t0, t2, selB);
+	P2					   = __byte_perm(t1, t3, selA);
+	P3					   = __byte_perm(t1, t3, selB);
+}
+
+
+}  // namespace scan_detail
+}  // namespace pars
