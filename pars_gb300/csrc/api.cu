@@ -9,6 +9,8 @@
 // then host checks that may re-issue work: capacity overflow (grow, rerun), the
 // escape path's speculation guard (rerun on the generic kernel), and a key range
 // the single sort pass cannot take (LSD passes, then k_pair).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,6 +32,11 @@ const void* scan_kernel(int path);
 int		   scan_fast_smem_bytes();
 int		   scan_fast_max_grid();
 int		   scan_ws_threads();
+int		   scan_ws_tile_bytes();
+struct WsArgs {
+	ScanArgs		   a;
+	unsigned long long rows_full;
+};
 int		   scan_ws_smem_bytes();
 const void* scan_ws_kernel(int path, bool brackets);
 const void* scan_fast_kernel(int path, bool brackets);
@@ -375,13 +382,57 @@ int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
 	return 0;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+	static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+	static bool								  tried = false;
+	if (!tried) {
+		tried = true;
+		void*							 p = nullptr;
+		cudaDriverEntryPointQueryResult q {};
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q)
+				== cudaSuccess
+			&& q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+		cudaGetLastError();
+	}
+	return fn;
+}
+
+// The document as a [rows][128] byte tensor (full rows only), 256-row boxes,
+// 128-byte swizzle.
+int make_row_map(pars_ctx* ctx, const uint8_t* base, uint64_t rows, CUtensorMap* map) {
+	std::memset(map, 0, sizeof *map);
+	if (rows == 0)
+		return 0;
+	auto enc = tensor_map_encoder();
+	if (!enc)
+		return fail(ctx, PARS_ECUDA, "cuTensorMapEncodeTiled unavailable");
+	const cuuint64_t dims[2]	= {128, rows};
+	const cuuint64_t strides[1] = {128};
+	const cuuint32_t box[2]		= {128, 256};
+	const cuuint32_t estr[2]	= {1, 1};
+	const CUresult	 r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(base), dims,
+							 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+							 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+							 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if (r != CUDA_SUCCESS) {
+		char msg[96];
+		std::snprintf(msg, sizeof msg, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(r));
+		ctx->err = msg;
+		return PARS_ECUDA;
+	}
+	return 0;
+}
+
 // `first` = first launch of a document: clears the result block + key histogram.
 int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true) {
 	const uint64_t o	 = reinterpret_cast<uintptr_t>(s.d_in) & 15u;
 	const uint8_t* base	 = s.d_in - o;
 	const uint64_t total = o + s.n;
-	const uint64_t ntiles = (total + kTileBytes - 1) / kTileBytes;
 	const bool	   fast	 = s.path != kPathGeneric;
+	const uint64_t tile	 = (fast && use_ws(s.path)) ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;
+	const uint64_t ntiles = (total + tile - 1) / tile;
 	const size_t tdesc = fast ? 2 * sizeof(uint4) : sizeof(TileDescG);  // fast: AGG + INCL words
 	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
 		return r;
@@ -420,7 +471,17 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	a.epoch		= next_epoch(ctx);
 	a.flags		= s.flags;
 	void* args[] = {&a};
-	if (fast) {
+	if (fast && use_ws(s.path)) {
+		const bool	br	 = pl->host.has_brackets != 0;
+		const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
+		WsArgs		wa {a, total / 128};
+		CUtensorMap map;
+		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+			return r;
+		void* wargs[] = {&wa, &map};
+		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br), dim3(grid), dim3(fast_threads(s.path)),
+									   wargs, fast_smem(s.path), s.st));
+	} else if (fast) {
 		const bool br	= pl->host.has_brackets != 0;
 		const int  grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
 		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br), dim3(grid), dim3(fast_threads(s.path)),

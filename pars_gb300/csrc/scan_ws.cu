@@ -1,24 +1,32 @@
 // scan_ws.cu — warp-specialised fused R1..R5 scan for plans whose lexical layer is
 // empty, a quote-parity automaton or a doubled-delimiter automaton (the CSV shape).
 //
-// Each CTA runs 16 worker warps and one manager warp on a static tile schedule
-// (CTA b owns 16 KiB tiles b, b+G, ...; cooperative launch keeps all CTAs
-// resident).  Nothing waits on a CTA-wide barrier inside the tile loop: the warps
-// hand work to each other through shared-memory mbarriers.
+// Data movement.  The document is viewed as a 2-D tensor of 128-byte rows and
+// streamed in 32 KiB tiles (256 rows) by TMA tensor copies with the 128-byte
+// swizzle, so each thread's 64 contiguous bytes (half a row) come out of shared
+// memory with conflict-free 16-byte loads in natural order.  The final partial
+// row (if any) is not covered by the tensor; its owner patches it from global
+// memory.  The ring has two slots: a slot is handed back as soon as the workers
+// have classified it, because phase B needs no input bytes from shared memory.
 //
-//   workers  A(k): wait for tile k's bytes (TMA ring), classify their 32-byte
-//                  words, scan (in-string parity, counts under both parity
-//                  hypotheses) across the warp, post the warp total, arrive TOT[k].
-//            B(k): wait BASE[k], add the manager's cross-warp prefix, resolve the
-//                  masks, write offsets / brackets / depth keys, arrive EMPTY[slot].
-//            order: A(0), A(1), B(0), A(2), B(1), ... so the manager's look-back
-//            for tile k overlaps the workers' classification of tile k+1.
-//   manager  per tile: wait TOT[k], scan the 16 warp totals, publish the tile's AGG
-//            look-back word, fold the predecessors' words, publish INCL, post the
-//            tile base, arrive BASE[k]; refill ring slots as EMPTY completes.
+// Schedule.  A cooperative persistent grid; CTA b owns tiles b, b+G, ... Each CTA
+// runs 16 worker warps and one manager warp; they hand work to each other through
+// mbarriers, never through a CTA-wide barrier inside the tile loop.
 //
-// Look-back words and their fold are those of scan_fast.cu (fast_common.cuh).
+//   workers  A(k): wait FULL[k%2]; classify their two 32-byte words; compose them,
+//                  scan the warp (in-string parity and counts under both parity
+//                  hypotheses), post the warp total; arrive TOT[k%2].
+//            B(k): wait BASE[k%2]; add the manager's cross-warp prefix; resolve the
+//                  masks; write offsets, brackets and depth keys.
+//            order A(0), A(1), B(0), A(2), B(1), ... so the manager's look-back
+//            for tile k overlaps the classification of tile k+1.
+//   manager  per tile: wait TOT[k%2] -> refill the slot with tile k+2 -> scan the
+//            16 warp totals -> publish AGG -> fold the look-back -> publish INCL ->
+//            post the tile base; arrive BASE[k%2].
+//
+// Look-back words and their fold are shared with scan_fast.cu (fast_common.cuh).
 // Reference semantics: include/pars/model/scan.hpp:33-72 and nest.hpp:55-76.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fast_common.cuh"
@@ -31,7 +39,9 @@ namespace {
 
 constexpr int kWorkers	 = 16;
 constexpr int kWsThreads = (kWorkers + 1) * 32;
-constexpr int kMgr		 = kWorkers;  // warp index of the manager
+constexpr int kMgr		 = kWorkers;				  // warp index of the manager
+constexpr int kWsTile	 = kWorkers * 32 * 64;		  // 32 KiB: 512 threads x 64 bytes
+constexpr int kWsRows	 = kWsTile / 128;			  // 256 rows of 128 bytes
 
 __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
@@ -51,6 +61,16 @@ __device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, std::uint32_t pari
 	return true;
 }
 
+// 2-D TMA: rows [row, row + 256) of the tensor into `dst` (1024-byte aligned).
+__device__ __forceinline__ void tma_rows(void* dst, const CUtensorMap* map, int row,
+										 std::uint64_t* bar) {
+	asm volatile(
+		"cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+		"[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+		"l"(reinterpret_cast<std::uint64_t>(map)), "r"(0), "r"(row), "r"(smem_addr(bar))
+		: "memory");
+}
+
 struct WsScratch {
 	std::uint32_t wtot[2][kWorkers][4];	 // worker warp aggregates (workers -> manager)
 	std::uint32_t wpre[2][kWorkers][4];	 // worker warp exclusive prefixes (manager -> workers)
@@ -61,21 +81,25 @@ struct WsScratch {
 	long long	  wext[4][kWorkers];
 };
 
+// Per-thread state of one tile between phase A and phase B (two words).
 struct WsFront {
-	std::uint32_t S, O, C, D;
-	std::uint32_t ex0, dd;
-	std::uint32_t ex[4];  // warp-exclusive scan value
-	std::uint32_t vm;
+	std::uint32_t S[2], O[2], C[2], D[2];
+	std::uint32_t ex0[2], dd[2];
+	std::uint32_t w0[4];  // element of word 0 (to derive word 1's prefix)
+	std::uint32_t ex[4];  // warp-exclusive thread prefix
+	std::uint32_t vm[2];
 };
 
+// Dynamic shared memory (window addresses): [scratch, histogram][pad to 64 KiB]
+// [class table 64 KiB][ring 2 x 32 KiB].  The table and ring start on 64 KiB and
+// 1 KiB boundaries of the shared window respectively.
 struct SmemWs {
-	static constexpr int kStage	   = 0;
-	static constexpr int kBars	   = kStage + kRing * kTileBytes;	// full[3] empty[3] tot[2] base[2]
-	static constexpr int kScratch  = kBars + 128;
+	static constexpr int kBars	   = 0;	 // full[2] tot[2] base[2]
+	static constexpr int kScratch  = 128;
 	static constexpr int kHist	   = (kScratch + static_cast<int>(sizeof(WsScratch)) + 127) & ~127;
 	static constexpr int kLowEnd   = kHist + 2 * kKeyWindow * 4;
 	static constexpr int kTblBytes = 256 * 256;
-	static constexpr int kBytes	   = kLowEnd + 65536 + kTblBytes;
+	static constexpr int kBytes	   = kLowEnd + 65535 + kTblBytes + 2 * kWsTile;
 };
 
 struct OpSum3 {
@@ -86,7 +110,6 @@ struct OpSum3 {
 	}
 };
 
-// Warp-inclusive scan (lane order); N lanes of the value used.
 template<class Op>
 __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane, int n_active) {
 #pragma unroll
@@ -103,19 +126,25 @@ __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane
 
 }  // namespace
 
+struct WsArgs {
+	ScanArgs		   a;
+	unsigned long long rows_full;  // 128-byte rows covered by the tensor map
+};
+
 template<int PATH, bool BR>
-__global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
+__global__ void __launch_bounds__(kWsThreads, 1)
+	k_scan_ws(const WsArgs wa, const __grid_constant__ CUtensorMap tmap) {
+	const ScanArgs& a = wa.a;
 	extern __shared__ __align__(128) unsigned char smem[];
-	unsigned char* ring		= smem + SmemWs::kStage;
 	std::uint64_t* full_bar = reinterpret_cast<std::uint64_t*>(smem + SmemWs::kBars);
-	std::uint64_t* empty_bar = full_bar + 3;
-	std::uint64_t* tot_bar	 = full_bar + 6;
-	std::uint64_t* base_bar	 = full_bar + 8;
-	WsScratch&	   sc		 = *reinterpret_cast<WsScratch*>(smem + SmemWs::kScratch);
-	unsigned int*  khist	 = reinterpret_cast<unsigned int*>(smem + SmemWs::kHist);
+	std::uint64_t* tot_bar	= full_bar + 2;
+	std::uint64_t* base_bar = full_bar + 4;
+	WsScratch&	   sc		= *reinterpret_cast<WsScratch*>(smem + SmemWs::kScratch);
+	unsigned int*  khist	= reinterpret_cast<unsigned int*>(smem + SmemWs::kHist);
 	const std::uint32_t win0	= smem_addr(smem);
 	const std::uint32_t tbl_win = (win0 + SmemWs::kLowEnd + 0xFFFFu) & ~0xFFFFu;
 	std::uint32_t*		tbl		= reinterpret_cast<std::uint32_t*>(smem + (tbl_win - win0));
+	unsigned char*		ring	= smem + (tbl_win - win0) + SmemWs::kTblBytes;
 
 	const int			tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const DevPlan*		P	= a.plan;
@@ -125,7 +154,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 	const std::uint32_t G	   = gridDim.x;
 	const std::uint32_t epoch  = a.epoch & 0x3FFFFFu;
 	const std::uint32_t ntiles = static_cast<std::uint32_t>(a.ntiles);
-	const unsigned long long doc_end = a.o + a.n;
+	const unsigned long long doc_end   = a.o + a.n;
+	const unsigned long long tensor_end = wa.rows_full * 128ull;  // bytes the TMA delivers
 	const std::uint32_t byte_base = a.carry_in ? static_cast<std::uint32_t>(a.carry_in->byte_base) : 0u;
 	const std::uint32_t init_state = a.carry_in ? (a.carry_in->fstate & 3u) : 0u;
 	const std::uint32_t base0[3] = {
@@ -137,17 +167,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 	if (BR)
 		for (int i = tid; i < 2 * kKeyWindow; i += kWsThreads) khist[i] = 0;
 	if (tid == 0) {
-		for (int s = 0; s < 3; ++s) {
+		for (int s = 0; s < 2; ++s) {
 			mbar_init(&full_bar[s], 1);
-			mbar_init(&empty_bar[s], kWorkers);
-		}
-		for (int p = 0; p < 2; ++p) {
-			mbar_init(&tot_bar[p], kWorkers);
-			mbar_init(&base_bar[p], 1);
+			mbar_init(&tot_bar[s], kWorkers);
+			mbar_init(&base_bar[s], 1);
 		}
 		fence_barrier_init();
 		sc.failed = 0;
-		if (tbl_win + SmemWs::kTblBytes > win0 + SmemWs::kBytes) {
+		if (tbl_win + SmemWs::kTblBytes + 2 * kWsTile > win0 + SmemWs::kBytes) {
 			record_error(res, kDevErrTimeout);
 			sc.failed = 1;
 		}
@@ -170,28 +197,39 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 		auto issue = [&](std::uint32_t k) {	 // lane 0
 			if (k >= n_mine)
 				return;
-			issued					 = k + 1;
-			const int				 s = static_cast<int>(k % 3);
-			const unsigned long long off = static_cast<unsigned long long>(tile_of(k)) * kTileBytes;
-			unsigned long long		 bytes = a.copy_end - off;
-			if (bytes > kTileBytes)
-				bytes = kTileBytes;
-			mbar_arrive_expect_tx(&full_bar[s], static_cast<std::uint32_t>(bytes));
-			bulk_g2s(ring + s * kTileBytes, a.base + off, static_cast<std::uint32_t>(bytes), &full_bar[s]);
+			issued	  = k + 1;
+			const int s = static_cast<int>(k & 1);
+			const unsigned long long row0 = static_cast<unsigned long long>(tile_of(k)) * kWsRows;
+			if (row0 >= wa.rows_full) {
+				// nothing of this tile is in the tensor: its workers read the tail bytes
+				// from global memory themselves
+				mbar_arrive(&full_bar[s]);
+			} else {
+				// rows past the tensor's end come back as zeros (and count as delivered)
+				mbar_arrive_expect_tx(&full_bar[s], kWsTile);
+				tma_rows(ring + s * kWsTile, &tmap, static_cast<int>(row0), &full_bar[s]);
+			}
 		};
-		if (lane == 0)
-			for (std::uint32_t k = 0; k < 3; ++k) issue(k);
+		if (lane == 0) {
+			if (wa.rows_full)
+				asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<std::uint64_t>(&tmap)) : "memory");
+			issue(0);
+			issue(1);
+		}
 		bool failed = false;
 		for (std::uint32_t k = 0; k < n_mine; ++k) {
 			const std::uint32_t t	= tile_of(k);
 			const int			buf = static_cast<int>(k & 1);
 			if (!failed && !mbar_wait(&tot_bar[buf], (k >> 1) & 1u, res))
 				failed = true;
+			failed = __shfl_sync(kFull, failed ? 1u : 0u, 0) != 0;
+			// the workers are done with slot k&1: load tile k+2 into it
+			if (lane == 0 && !failed)
+				issue(k + 2);
 			std::uint32_t s_t = init_state, base[3] = {base0[0], base0[1], base0[2]};
 			uint4		  agg = make_uint4(0, 0, 0, 0);
 			std::uint32_t tile_elem = kIdent;
 			if (!failed) {
-				// cross-warp exclusive scan of the 16 worker aggregates
 				std::uint32_t w[4] = {0, 0, 0, 0};
 				if (lane < kWorkers)
 #pragma unroll
@@ -263,7 +301,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 									bad = true;
 									break;
 								}
-								__nanosleep(32);
+								__nanosleep(20);
 								lbv[i] = ld128_relaxed(src);
 							}
 						}
@@ -364,27 +402,22 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 			__syncwarp();
 			if (lane == 0)
 				mbar_arrive(&base_bar[buf]);
-			// ring refill: tile k-1's slot takes tile k+2 once its workers are done
-			if (lane == 0 && !failed && k >= 1 && k + 2 < n_mine) {
-				if (mbar_wait(&empty_bar[(k - 1) % 3], ((k - 1) / 3) & 1u, res))
-					issue(k + 2);
-				else
-					failed = true;
-			}
-			failed = __shfl_sync(kFull, failed ? 1u : 0u, 0) != 0;
 		}
 		// drain: every issued copy must land before the CTA exits
 		if (lane == 0)
-			for (std::uint32_t k = (issued > 3 ? issued - 3 : 0); k < issued; ++k)
-				mbar_wait(&full_bar[k % 3], (k / 3) & 1u, res);
+			for (std::uint32_t k = (issued > 2 ? issued - 2 : 0); k < issued; ++k)
+				mbar_wait(&full_bar[k & 1], (k >> 1) & 1u, res);
 	} else {
 		// ================================================================ workers ====
 		const std::uint32_t wtid	 = static_cast<std::uint32_t>(tid);	 // 0..511
 		const std::uint32_t tbl_lane = tbl_win + 4u * lane;
-		const std::uint32_t sw		 = (wtid >> 2) & 1u;
-		const std::uint32_t selA	 = sw ? 0x1054u : 0x5410u;
-		const std::uint32_t selB	 = sw ? 0x3276u : 0x7632u;
-		const std::uint8_t	delim	 = P->delim;
+		const std::uint32_t row		 = wtid >> 1;							 // row of this thread's 64 bytes
+		const std::uint32_t half	 = wtid & 1u;
+		std::uint32_t		chunk_off[4];									 // swizzled 16-byte chunks
+#pragma unroll
+		for (int c = 0; c < 4; ++c)
+			chunk_off[c] = row * 128u + ((((half << 2) + c) ^ (row & 7u)) << 4);
+		const std::uint8_t	delim	   = P->delim;
 		const bool			want_pairs = (a.flags & 1u) != 0;
 		const bool			want_chars = (a.flags & 4u) != 0;
 		const bool			want_mask  = (a.flags & 8u) != 0 && a.mask;
@@ -393,85 +426,141 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 
 		auto phase_a = [&](std::uint32_t k, WsFront& F) -> bool {
 			const std::uint32_t t	= tile_of(k);
-			const int			s	= static_cast<int>(k % 3);
-			const int			buf = static_cast<int>(k & 1);
-			if (!mbar_wait(&full_bar[s], (k / 3) & 1u, res)) {
+			const int			s	= static_cast<int>(k & 1);
+			const int			buf = s;
+			if (!mbar_wait(&full_bar[s], (k >> 1) & 1u, res)) {
 				sc.failed = 1;
 				return false;
 			}
-			const unsigned char*	 stage = ring + s * kTileBytes;
-			const unsigned long long q0	   = static_cast<unsigned long long>(t) * kTileBytes + 32u * wtid;
-			const bool interior = static_cast<unsigned long long>(t) * kTileBytes >= a.o
-							   && static_cast<unsigned long long>(t + 1) * kTileBytes <= doc_end;
-			std::uint32_t vm = 0xFFFFFFFFu;
-			int			  lo = 0, hi = 32;
-			if (!interior) {
-				if (q0 < a.o)
-					lo = (a.o - q0) > 32 ? 32 : static_cast<int>(a.o - q0);
-				if (doc_end < q0 + 32)
-					hi = doc_end <= q0 ? 0 : static_cast<int>(doc_end - q0);
-				if (hi < lo)
-					hi = lo;
-				vm = bit_range(lo, hi);
-			}
-			F.vm = vm;
-			std::uint32_t r[8];
-			{
-				const uint4* p = reinterpret_cast<const uint4*>(stage + 32 * wtid);
-				const uint4	 x = p[sw];
-				const uint4	 y = p[sw ^ 1u];
-				r[0] = x.x;
-				r[1] = x.y;
-				r[2] = x.z;
-				r[3] = x.w;
-				r[4] = y.x;
-				r[5] = y.y;
-				r[6] = y.z;
-				r[7] = y.w;
-			}
-			std::uint32_t S, O, C, D;
-			classify_word(r, tbl_lane, selA, selB, S, O, C, D);
-			if (!interior) {
-				S &= vm;
-				O &= vm;
-				C &= vm;
-				D &= vm;
-			}
-			F.S = S;
-			F.O = O;
-			F.C = C;
-			F.D = D;
-			std::uint32_t v[4];
-			if (PATH == kPathNone) {
-				F.ex0 = F.dd = 0;
-				v[0] = __popc(S);
-				v[1] = 0;
-				v[2] = BR ? __popc(O) : 0u;
-				v[3] = BR ? __popc(C) : 0u;
-				warp_scan(v, OpSum3(), lane, 32);
-			} else {
-				const std::uint32_t ex0 = prefix_xor32(D) ^ D;
-				std::uint32_t		dd	= 0;
-				if (PATH == kPathDoubled) {
-					std::uint32_t prev	= __shfl_up_sync(kFull, D >> 31, 1);
-					const bool	  first = (q0 + lo == a.o);
-					if (first) {
-						prev = a.carry_in ? (a.carry_in->last_delim & 1u) : 0u;
-					} else if (lane == 0 && vm != 0) {
-						prev = (wtid > 0 ? stage[32 * wtid - 1] : a.base[q0 - 1]) == delim ? 1u : 0u;
-					}
-					dd = D & ((D << 1) | ((prev & 1u) << lo));
+			unsigned char*			 stage = ring + s * kWsTile;
+			const unsigned long long q0	   = static_cast<unsigned long long>(t) * kWsTile + 64u * wtid;
+			// the tail past the tensor's last full row is read from global memory
+			if (q0 + 64 > tensor_end && q0 < doc_end) {
+				for (int b = 0; b < 64; ++b) {
+					const unsigned long long q = q0 + b;
+					if (q >= tensor_end && q < doc_end)
+						stage[chunk_off[b >> 4] + (b & 15)] = a.base[q];
 				}
-				const std::uint32_t m0 = ex0 | dd, m1 = ~ex0 | dd;
-				v[0] = __popc(S & ~m0) | (__popc(S & ~m1) << 16);
-				v[1] = __popc(D) & 1u;
-				v[2] = BR ? (__popc(O & ~m0) | (__popc(O & ~m1) << 16)) : 0u;
-				v[3] = BR ? (__popc(C & ~m0) | (__popc(C & ~m1) << 16)) : 0u;
-				F.ex0 = ex0;
-				F.dd  = dd;
-				warp_scan(v, OpParity(), lane, 32);
 			}
-			// v is now warp-inclusive; keep the warp-exclusive part
+			const bool interior = static_cast<unsigned long long>(t) * kWsTile >= a.o
+							   && static_cast<unsigned long long>(t + 1) * kWsTile <= doc_end;
+			std::uint32_t v[4], w0[4] = {0, 0, 0, 0};
+			std::uint32_t pdelim = 0;  // previous byte a delimiter (doubled path)
+			if (PATH == kPathDoubled) {
+				// byte before this thread's first byte: the previous lane's last bit, or memory
+				const bool first = (q0 <= a.o);
+				if (lane == 0 && !first)
+					pdelim = a.base[q0 - 1] == delim ? 1u : 0u;
+			}
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const unsigned long long qw = q0 + 32u * h;
+				std::uint32_t			 vm = 0xFFFFFFFFu;
+				int						 lo = 0, hi = 32;
+				if (!interior) {
+					if (qw < a.o)
+						lo = (a.o - qw) > 32 ? 32 : static_cast<int>(a.o - qw);
+					if (doc_end < qw + 32)
+						hi = doc_end <= qw ? 0 : static_cast<int>(doc_end - qw);
+					if (hi < lo)
+						hi = lo;
+					vm = bit_range(lo, hi);
+				}
+				F.vm[h] = vm;
+				std::uint32_t r[8];
+				{
+					const uint4 x = *reinterpret_cast<const uint4*>(stage + chunk_off[2 * h]);
+					const uint4 y = *reinterpret_cast<const uint4*>(stage + chunk_off[2 * h + 1]);
+					r[0] = x.x;
+					r[1] = x.y;
+					r[2] = x.z;
+					r[3] = x.w;
+					r[4] = y.x;
+					r[5] = y.y;
+					r[6] = y.z;
+					r[7] = y.w;
+				}
+				std::uint32_t S, O, C, D;
+				classify_word(r, tbl_lane, 0x5410u, 0x7632u, S, O, C, D);
+				if (!interior) {
+					S &= vm;
+					O &= vm;
+					C &= vm;
+					D &= vm;
+				}
+				F.S[h] = S;
+				F.O[h] = O;
+				F.C[h] = C;
+				F.D[h] = D;
+				std::uint32_t e[4];
+				if (PATH == kPathNone) {
+					F.ex0[h] = F.dd[h] = 0;
+					e[0]			   = __popc(S);
+					e[1]			   = 0;
+					e[2]			   = BR ? __popc(O) : 0u;
+					e[3]			   = BR ? __popc(C) : 0u;
+				} else {
+					F.ex0[h] = prefix_xor32(D) ^ D;
+					F.dd[h]	 = 0;  // doubled path: completed once both words are known
+					e[0]	 = 0;
+					e[1]	 = __popc(D) & 1u;
+					e[2] = e[3] = 0;
+				}
+				if (h == 0)
+#pragma unroll
+					for (int i = 0; i < 4; ++i) w0[i] = e[i];
+				else
+#pragma unroll
+					for (int i = 0; i < 4; ++i) v[i] = e[i];
+			}
+			if (PATH == kPathParity || PATH == kPathDoubled) {
+				std::uint32_t dd0 = 0, dd1 = 0;
+				if (PATH == kPathDoubled) {
+					// previous-byte-delimiter bits: word 1 takes word 0's last byte; word 0
+					// takes the previous thread's last byte (lane - 1, or memory for lane 0)
+					std::uint32_t prev = __shfl_up_sync(kFull, F.D[1] >> 31, 1);
+					const bool	  first = (q0 <= a.o);
+					if (lane == 0)
+						prev = pdelim;
+					if (first) {
+						// the document (or chunk) starts inside this thread's bytes
+						const int lo0 = static_cast<int>(a.o - q0);	 // 0..63
+						prev		  = a.carry_in ? (a.carry_in->last_delim & 1u) : 0u;
+						if (lo0 < 32) {
+							dd0 = F.D[0] & ((F.D[0] << 1) | (prev << lo0));
+							dd1 = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
+						} else {
+							dd0 = 0;
+							dd1 = F.D[1] & ((F.D[1] << 1) | (prev << (lo0 - 32)));
+						}
+					} else {
+						dd0 = F.D[0] & ((F.D[0] << 1) | (prev & 1u));
+						dd1 = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
+					}
+				}
+				F.dd[0] = dd0;
+				F.dd[1] = dd1;
+				// counts of each word under both parity hypotheses
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					const std::uint32_t m0 = F.ex0[h] | F.dd[h], m1 = ~F.ex0[h] | F.dd[h];
+					std::uint32_t*		e  = h == 0 ? w0 : v;
+					e[0] = __popc(F.S[h] & ~m0) | (__popc(F.S[h] & ~m1) << 16);
+					if (BR) {
+						e[2] = __popc(F.O[h] & ~m0) | (__popc(F.O[h] & ~m1) << 16);
+						e[3] = __popc(F.C[h] & ~m0) | (__popc(F.C[h] & ~m1) << 16);
+					}
+				}
+				OpParity()(w0, v);	// thread element = word 0 then word 1
+			} else {
+				OpSum3()(w0, v);
+			}
+#pragma unroll
+			for (int i = 0; i < 4; ++i) F.w0[i] = w0[i];
+			if (PATH == kPathNone)
+				warp_scan(v, OpSum3(), lane, 32);
+			else
+				warp_scan(v, OpParity(), lane, 32);
 #pragma unroll
 			for (int i = 0; i < 4; ++i) {
 				const std::uint32_t e = __shfl_up_sync(kFull, v[i], 1);
@@ -488,129 +577,135 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 
 		auto phase_b = [&](std::uint32_t k, const WsFront& F) -> bool {
 			const std::uint32_t t	= tile_of(k);
-			const int			s	= static_cast<int>(k % 3);
 			const int			buf = static_cast<int>(k & 1);
 			if (!mbar_wait(&base_bar[buf], (k >> 1) & 1u, res) || sc.failed) {
 				sc.failed = 1;
 				return false;
 			}
-			const unsigned char*	 stage = ring + s * kTileBytes;
-			const unsigned long long q0	   = static_cast<unsigned long long>(t) * kTileBytes + 32u * wtid;
-			const std::uint32_t		 s_t   = sc.state[buf];
-			const std::uint32_t		 p_t   = (s_t >> 1) & 1u;
-			// this word's prefix = manager's cross-warp prefix, then the warp prefix
-			std::uint32_t pre[4];
+			const unsigned long long q0	 = static_cast<unsigned long long>(t) * kWsTile + 64u * wtid;
+			const std::uint32_t		 s_t = sc.state[buf];
+			const std::uint32_t		 p_t = (s_t >> 1) & 1u;
+			std::uint32_t			 pre[4];
 #pragma unroll
 			for (int i = 0; i < 4; ++i) pre[i] = sc.wpre[buf][warp][i];
-			std::uint32_t ex[4] = {F.ex[0], F.ex[1], F.ex[2], F.ex[3]};
-			std::uint32_t off[3];
-			std::uint32_t p_w = 0;
-			if (PATH == kPathNone) {
-				OpSum3()(pre, ex);
-				off[0] = ex[0];
-				off[1] = ex[2];
-				off[2] = ex[3];
-			} else {
-				OpParity()(pre, ex);
-				p_w	   = p_t ^ ex[1];
-				off[0] = half16(ex[0], p_t);
-				off[1] = half16(ex[2], p_t);
-				off[2] = half16(ex[3], p_t);
-			}
 			const std::uint32_t base[3] = {sc.base[buf][0], sc.base[buf][1], sc.base[buf][2]};
-			const std::uint32_t vm		= F.vm;
-			std::uint32_t		mask	= 0;
-			if (PATH != kPathNone)
-				mask = ((F.ex0 ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd) & vm;
-			// the worker holding the document's last byte records the end state
-			if (vm != 0 && doc_end <= q0 + 32 && doc_end > q0) {
-				const int			hi		  = static_cast<int>(doc_end - q0);
-				const std::uint32_t elem	  = 1u | ((__popc(F.D) & 1u) << 2);
-				const std::uint32_t endstate  = PATH == kPathNone ? 0u : apply_fast(elem, p_w << 1);
-				const std::uint32_t last_flag = (F.D >> (hi - 1)) & 1u;
-				const std::uint32_t unclosed  = PATH == kPathNone ? 0u : (((endstate >> 1) & 1u) | last_flag);
-				res->unclosed				  = unclosed;
-				if (a.carry_out) {
-					a.carry_out->fstate		 = endstate;
-					a.carry_out->last_delim	 = last_flag;
-					a.carry_out->last_toggle = last_flag;
-					a.carry_out->unclosed	 = unclosed;
+			// prefixes of word 0 and word 1
+			std::uint32_t p0[4] = {F.ex[0], F.ex[1], F.ex[2], F.ex[3]};
+			if (PATH == kPathNone)
+				OpSum3()(pre, p0);
+			else
+				OpParity()(pre, p0);
+			std::uint32_t p1[4] = {F.w0[0], F.w0[1], F.w0[2], F.w0[3]};
+			std::uint32_t p0c[4] = {p0[0], p0[1], p0[2], p0[3]};
+			if (PATH == kPathNone)
+				OpSum3()(p0c, p1);
+			else
+				OpParity()(p0c, p1);
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const std::uint32_t* pw = h == 0 ? p0 : p1;
+				const unsigned long long qw = q0 + 32u * h;
+				const std::uint32_t	 vm	= F.vm[h];
+				std::uint32_t		 off[3], p_w = 0;
+				if (PATH == kPathNone) {
+					off[0] = pw[0];
+					off[1] = pw[2];
+					off[2] = pw[3];
+				} else {
+					p_w	   = p_t ^ pw[1];
+					off[0] = half16(pw[0], p_t);
+					off[1] = half16(pw[2], p_t);
+					off[2] = half16(pw[3], p_t);
 				}
-			}
-			std::uint32_t		m	 = F.S & ~mask;
-			std::uint32_t		si	 = base[0] + off[0];
-			const std::uint32_t pos0 = byte_base + static_cast<std::uint32_t>(q0 - a.o);
-			const unsigned char* wb	 = stage + 32 * wtid;
-			if (!BR) {
-				if (si + static_cast<std::uint32_t>(__popc(m)) <= cap_s && !want_chars && !want_pairs) {
-					std::uint32_t* out = a.pos + si;
-					while (m) {
-						const int j = __ffs(m) - 1;
-						m &= m - 1;
-						*out++ = pos0 + j;
+				std::uint32_t mask = 0;
+				if (PATH != kPathNone)
+					mask = ((F.ex0[h] ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd[h]) & vm;
+				if (vm != 0 && doc_end <= qw + 32 && doc_end > qw) {
+					const int			hi		  = static_cast<int>(doc_end - qw);
+					const std::uint32_t elem	  = 1u | ((__popc(F.D[h]) & 1u) << 2);
+					const std::uint32_t endstate  = PATH == kPathNone ? 0u : apply_fast(elem, p_w << 1);
+					const std::uint32_t last_flag = (F.D[h] >> (hi - 1)) & 1u;
+					const std::uint32_t unclosed  = PATH == kPathNone ? 0u : (((endstate >> 1) & 1u) | last_flag);
+					res->unclosed				  = unclosed;
+					if (a.carry_out) {
+						a.carry_out->fstate		 = endstate;
+						a.carry_out->last_delim	 = last_flag;
+						a.carry_out->last_toggle = last_flag;
+						a.carry_out->unclosed	 = unclosed;
+					}
+				}
+				std::uint32_t		m	 = F.S[h] & ~mask;
+				std::uint32_t		si	 = base[0] + off[0];
+				const std::uint32_t pos0 = byte_base + static_cast<std::uint32_t>(qw - a.o);
+				const unsigned char* gb	 = a.base + qw;	 // input bytes (global, L2-resident)
+				if (!BR) {
+					if (si + static_cast<std::uint32_t>(__popc(m)) <= cap_s && !want_chars && !want_pairs) {
+						std::uint32_t* out = a.pos + si;
+						while (m) {
+							const int j = __ffs(m) - 1;
+							m &= m - 1;
+							*out++ = pos0 + j;
+						}
+					} else {
+						while (m) {
+							const int j = __ffs(m) - 1;
+							m &= m - 1;
+							if (si < cap_s) {
+								a.pos[si] = pos0 + j;
+								if (want_chars)
+									a.chars[si] = gb[j];
+								if (want_pairs)
+									a.pair[si] = -1;
+							}
+							++si;
+						}
 					}
 				} else {
+					const std::uint32_t selo = F.O[h] & ~mask;
+					const std::uint32_t selc = F.C[h] & ~mask;
+					const std::uint32_t no0	 = base[1] + off[1];
+					const std::uint32_t nc0	 = base[2] + off[2];
+					std::uint32_t		bi	 = no0 + nc0;
+					long long			dep	 = static_cast<long long>(no0) - static_cast<long long>(nc0);
+					const std::uint32_t bm	 = selo | selc;
 					while (m) {
 						const int j = __ffs(m) - 1;
 						m &= m - 1;
+						const std::uint32_t pos = pos0 + j;
 						if (si < cap_s) {
-							a.pos[si] = pos0 + j;
+							a.pos[si] = pos;
 							if (want_chars)
-								a.chars[si] = wb[j];
+								a.chars[si] = gb[j];
 							if (want_pairs)
 								a.pair[si] = -1;
+						}
+						if ((bm >> j) & 1u) {
+							const bool		op	= (selo >> j) & 1u;
+							const long long key = op ? dep : dep - 1;
+							dep += op ? 1 : -1;
+							if (bi < cap_b) {
+								a.bpos[bi]	= pos;
+								a.bchar[bi] = gb[j];
+								a.bsi[bi]	= si;
+								a.depth[bi] = static_cast<std::int32_t>(key);
+							}
+							++bi;
+							ext_min_bal = dep < ext_min_bal ? dep : ext_min_bal;
+							ext_max_bal = dep > ext_max_bal ? dep : ext_max_bal;
+							ext_min_key = key < ext_min_key ? key : ext_min_key;
+							ext_max_key = key > ext_max_key ? key : ext_max_key;
+							any_keys	= true;
+							if (key >= -kKeyWindow && key < kKeyWindow)
+								atomicAdd(&khist[key + kKeyWindow], 1u);
+							else
+								atomicOr(&res->keys_oob, 1u);
 						}
 						++si;
 					}
 				}
-			} else {
-				const std::uint32_t selo = F.O & ~mask;
-				const std::uint32_t selc = F.C & ~mask;
-				const std::uint32_t no0	 = base[1] + off[1];
-				const std::uint32_t nc0	 = base[2] + off[2];
-				std::uint32_t		bi	 = no0 + nc0;
-				long long			dep	 = static_cast<long long>(no0) - static_cast<long long>(nc0);
-				const std::uint32_t bm	 = selo | selc;
-				while (m) {
-					const int j = __ffs(m) - 1;
-					m &= m - 1;
-					const std::uint32_t pos = pos0 + j;
-					if (si < cap_s) {
-						a.pos[si] = pos;
-						if (want_chars)
-							a.chars[si] = wb[j];
-						if (want_pairs)
-							a.pair[si] = -1;
-					}
-					if ((bm >> j) & 1u) {
-						const bool		op	= (selo >> j) & 1u;
-						const long long key = op ? dep : dep - 1;
-						dep += op ? 1 : -1;
-						if (bi < cap_b) {
-							a.bpos[bi]	= pos;
-							a.bchar[bi] = wb[j];
-							a.bsi[bi]	= si;
-							a.depth[bi] = static_cast<std::int32_t>(key);
-						}
-						++bi;
-						ext_min_bal = dep < ext_min_bal ? dep : ext_min_bal;
-						ext_max_bal = dep > ext_max_bal ? dep : ext_max_bal;
-						ext_min_key = key < ext_min_key ? key : ext_min_key;
-						ext_max_key = key > ext_max_key ? key : ext_max_key;
-						any_keys	= true;
-						if (key >= -kKeyWindow && key < kKeyWindow)
-							atomicAdd(&khist[key + kKeyWindow], 1u);
-						else
-							atomicOr(&res->keys_oob, 1u);
-					}
-					++si;
-				}
+				if (want_mask && vm != 0)
+					a.mask[(byte_base + static_cast<std::uint32_t>(qw - a.o)) >> 5] = mask;
 			}
-			if (want_mask && vm != 0)
-				a.mask[(byte_base + static_cast<std::uint32_t>(q0 - a.o)) >> 5] = mask;
-			__syncwarp();
-			if (lane == 0)
-				mbar_arrive(&empty_bar[s]);
 			return true;
 		};
 
@@ -670,7 +765,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_scan_ws(const ScanArgs a) {
 	}
 }
 
-#define PARS_INST(P, B) template __global__ void k_scan_ws<P, B>(const ScanArgs);
+#define PARS_INST(P, B) \
+	template __global__ void k_scan_ws<P, B>(const WsArgs, const __grid_constant__ CUtensorMap);
 PARS_INST(kPathNone, false)
 PARS_INST(kPathNone, true)
 PARS_INST(kPathParity, false)
@@ -685,6 +781,10 @@ int scan_ws_threads() {
 
 int scan_ws_smem_bytes() {
 	return SmemWs::kBytes;
+}
+
+int scan_ws_tile_bytes() {
+	return kWsTile;
 }
 
 const void* scan_ws_kernel(int path, bool brackets) {
