@@ -20,7 +20,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/pars_gb300.h"
+#include "pars_gb300.h"
 #include "device.cuh"
 #include "pars_internal.h"
 
