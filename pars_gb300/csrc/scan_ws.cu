@@ -7,7 +7,8 @@
 // memory with conflict-free 16-byte loads in natural order.  The final partial
 // row (if any) is not covered by the tensor; its owner patches it from global
 // memory.  The ring has two slots: a slot is handed back as soon as the workers
-// have classified it, because phase B needs no input bytes from shared memory.
+// have classified it, because phase B needs no input bytes from shared memory
+// (the few bytes it copies out come from global memory, still in L2).
 //
 // Schedule.  A cooperative persistent grid; CTA b owns tiles b, b+G, ... Each CTA
 // runs 16 worker warps and one manager warp; they hand work to each other through
@@ -15,14 +16,20 @@
 //
 //   workers  A(k): wait FULL[k%2]; classify their two 32-byte words; compose them,
 //                  scan the warp (in-string parity and counts under both parity
-//                  hypotheses), post the warp total; arrive TOT[k%2].
-//            B(k): wait BASE[k%2]; add the manager's cross-warp prefix; resolve the
+//                  hypotheses), post the warp total; arrive TOT[k%4].  Warp 0 then
+//                  waits for TOT[k%4] and refills the slot with tile k+2.
+//            B(k): wait BASE[k%4]; add the manager's cross-warp prefix; resolve the
 //                  masks; write offsets, brackets and depth keys.
-//            order A(0), A(1), B(0), A(2), B(1), ... so the manager's look-back
-//            for tile k overlaps the classification of tile k+1.
-//   manager  per tile: wait TOT[k%2] -> refill the slot with tile k+2 -> scan the
-//            16 warp totals -> publish AGG -> fold the look-back -> publish INCL ->
-//            post the tile base; arrive BASE[k%2].
+//            order A(0), A(1), A(2), then A(k+3), B(k) for k = 0, 1, ...: the
+//            class planes of four tiles live in registers, so a tile's totals are
+//            published three tiles before its base is needed.
+//   manager  agg(k):  wait TOT[k%4] -> scan the 16 warp totals -> publish AGG.
+//            fold(k): fold the look-back -> publish INCL -> post the tile base;
+//                     arrive BASE[k%4].  Order agg(0), then agg(k+1), fold(k).
+//
+// Running A ahead matters because the CTAs of one wave drift apart by several
+// tile times: with A and B in lock step, each fold waited for the slowest
+// predecessor in its wave.
 //
 // Look-back words and their fold are shared with scan_fast.cu (fast_common.cuh).
 // Reference semantics: include/pars/model/scan.hpp:33-72 and nest.hpp:55-76.
@@ -42,6 +49,8 @@ constexpr int kWsThreads = (kWorkers + 1) * 32;
 constexpr int kMgr		 = kWorkers;				  // warp index of the manager
 constexpr int kWsTile	 = kWorkers * 32 * 64;		  // 32 KiB: 512 threads x 64 bytes
 constexpr int kWsRows	 = kWsTile / 128;			  // 256 rows of 128 bytes
+constexpr int kAhead	 = 3;						  // workers run phase A this many tiles ahead of B
+constexpr int kBufs		 = 4;						  // hand-off buffers (>= kAhead + 1)
 
 __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
@@ -72,29 +81,30 @@ __device__ __forceinline__ void tma_rows(void* dst, const CUtensorMap* map, int 
 }
 
 struct WsScratch {
-	std::uint32_t wtot[2][kWorkers][4];	 // worker warp aggregates (workers -> manager)
-	std::uint32_t wpre[2][kWorkers][4];	 // worker warp exclusive prefixes (manager -> workers)
-	std::uint32_t state[2];				 // tile incoming state
-	std::uint32_t base[2][3];			 // tile base counts
+	uint4		  tagg[kBufs];				 // tile aggregates between agg and fold (manager)
+	std::uint32_t wtot[kBufs][kWorkers][4];	 // worker warp aggregates (workers -> manager)
+	std::uint32_t wpre[kBufs][kWorkers][4];	 // worker warp exclusive prefixes (manager -> workers)
+	std::uint32_t state[kBufs];				 // tile incoming state
+	std::uint32_t base[kBufs][3];			 // tile base counts
 	std::uint32_t failed;
 	std::uint32_t any_br;
 	long long	  wext[4][kWorkers];
 };
 
-// Per-thread state of one tile between phase A and phase B (two words).
+// Per-thread state of one tile between phase A and phase B (two words): the class
+// planes, the doubled path's "previous byte was a delimiter" bits, and the
+// warp-exclusive prefix of the thread.  Everything else is recomputed in B.
 struct WsFront {
-	std::uint32_t S[2], O[2], C[2], D[2];
-	std::uint32_t ex0[2], dd[2];
-	std::uint32_t w0[4];  // element of word 0 (to derive word 1's prefix)
-	std::uint32_t ex[4];  // warp-exclusive thread prefix
-	std::uint32_t vm[2];
+	std::uint32_t S[2], D[2], dd[2];
+	std::uint32_t O[2], C[2];  // bracket planes (unused without brackets)
+	std::uint32_t ex[4];
 };
 
 // Dynamic shared memory (window addresses): [scratch, histogram][pad to 64 KiB]
 // [class table 64 KiB][ring 2 x 32 KiB].  The table and ring start on 64 KiB and
 // 1 KiB boundaries of the shared window respectively.
 struct SmemWs {
-	static constexpr int kBars	   = 0;	 // full[2] tot[2] base[2]
+	static constexpr int kBars	   = 0;	 // full[2] tot[4] base[4]
 	static constexpr int kScratch  = 128;
 	static constexpr int kHist	   = (kScratch + static_cast<int>(sizeof(WsScratch)) + 127) & ~127;
 	static constexpr int kLowEnd   = kHist + 2 * kKeyWindow * 4;
@@ -138,7 +148,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	extern __shared__ __align__(128) unsigned char smem[];
 	std::uint64_t* full_bar = reinterpret_cast<std::uint64_t*>(smem + SmemWs::kBars);
 	std::uint64_t* tot_bar	= full_bar + 2;
-	std::uint64_t* base_bar = full_bar + 4;
+	std::uint64_t* base_bar = full_bar + 2 + kBufs;
 	WsScratch&	   sc		= *reinterpret_cast<WsScratch*>(smem + SmemWs::kScratch);
 	unsigned int*  khist	= reinterpret_cast<unsigned int*>(smem + SmemWs::kHist);
 	const std::uint32_t win0	= smem_addr(smem);
@@ -167,10 +177,10 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	if (BR)
 		for (int i = tid; i < 2 * kKeyWindow; i += kWsThreads) khist[i] = 0;
 	if (tid == 0) {
-		for (int s = 0; s < 2; ++s) {
-			mbar_init(&full_bar[s], 1);
-			mbar_init(&tot_bar[s], kWorkers);
-			mbar_init(&base_bar[s], 1);
+		for (int s = 0; s < 2; ++s) mbar_init(&full_bar[s], 1);
+		for (int p = 0; p < kBufs; ++p) {
+			mbar_init(&tot_bar[p], kWorkers);
+			mbar_init(&base_bar[p], 1);
 		}
 		fence_barrier_init();
 		sc.failed = 0;
@@ -193,183 +203,167 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 
 	if (warp == kMgr) {
 		// ================================================================ manager ====
-		std::uint32_t issued = 0;
-		auto issue = [&](std::uint32_t k) {	 // lane 0
+		bool failed = false;
+		// agg(k): scan the 16 warp totals of tile k, hand the warp prefixes back and
+		// publish the tile's AGG word (tile 0 publishes its INCL word directly).
+		auto agg_step = [&](std::uint32_t k) {
 			if (k >= n_mine)
 				return;
-			issued	  = k + 1;
-			const int s = static_cast<int>(k & 1);
-			const unsigned long long row0 = static_cast<unsigned long long>(tile_of(k)) * kWsRows;
-			if (row0 >= wa.rows_full) {
-				// nothing of this tile is in the tensor: its workers read the tail bytes
-				// from global memory themselves
-				mbar_arrive(&full_bar[s]);
-			} else {
-				// rows past the tensor's end come back as zeros (and count as delivered)
-				mbar_arrive_expect_tx(&full_bar[s], kWsTile);
-				tma_rows(ring + s * kWsTile, &tmap, static_cast<int>(row0), &full_bar[s]);
-			}
-		};
-		if (lane == 0) {
-			if (wa.rows_full)
-				asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<std::uint64_t>(&tmap)) : "memory");
-			issue(0);
-			issue(1);
-		}
-		bool failed = false;
-		for (std::uint32_t k = 0; k < n_mine; ++k) {
 			const std::uint32_t t	= tile_of(k);
-			const int			buf = static_cast<int>(k & 1);
-			if (!failed && !mbar_wait(&tot_bar[buf], (k >> 1) & 1u, res))
+			const int			buf = static_cast<int>(k % kBufs);
+			if (!failed && !mbar_wait(&tot_bar[buf], (k / kBufs) & 1u, res))
 				failed = true;
 			failed = __shfl_sync(kFull, failed ? 1u : 0u, 0) != 0;
-			// the workers are done with slot k&1: load tile k+2 into it
-			if (lane == 0 && !failed)
-				issue(k + 2);
-			std::uint32_t s_t = init_state, base[3] = {base0[0], base0[1], base0[2]};
-			uint4		  agg = make_uint4(0, 0, 0, 0);
-			std::uint32_t tile_elem = kIdent;
-			if (!failed) {
-				std::uint32_t w[4] = {0, 0, 0, 0};
-				if (lane < kWorkers)
+			if (failed)
+				return;
+			std::uint32_t w[4] = {0, 0, 0, 0};
+			if (lane < kWorkers)
 #pragma unroll
-					for (int i = 0; i < 4; ++i) w[i] = sc.wtot[buf][lane][i];
-				if (PATH == kPathNone)
-					warp_scan(w, OpSum3(), lane, kWorkers);
-				else
-					warp_scan(w, OpParity(), lane, kWorkers);
-				std::uint32_t we[4];
+				for (int i = 0; i < 4; ++i) w[i] = sc.wtot[buf][lane][i];
+			if (PATH == kPathNone)
+				warp_scan(w, OpSum3(), lane, kWorkers);
+			else
+				warp_scan(w, OpParity(), lane, kWorkers);
+			std::uint32_t we[4];
 #pragma unroll
-				for (int i = 0; i < 4; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
-				if (lane == 0)
+			for (int i = 0; i < 4; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
+			if (lane == 0)
 #pragma unroll
-					for (int i = 0; i < 4; ++i) we[i] = 0;
-				if (lane < kWorkers)
+				for (int i = 0; i < 4; ++i) we[i] = 0;
+			if (lane < kWorkers)
 #pragma unroll
-					for (int i = 0; i < 4; ++i) sc.wpre[buf][lane][i] = we[i];
-				std::uint32_t tot[4];
+				for (int i = 0; i < 4; ++i) sc.wpre[buf][lane][i] = we[i];
+			std::uint32_t tot[4];
 #pragma unroll
-				for (int i = 0; i < 4; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
-				if (PATH == kPathNone) {
-					agg = make_uint4(tot[0], tot[2], tot[3], 0u);
-				} else {
-					tile_elem = 1u | (tot[1] << 2);
-					agg		  = make_uint4(tot[0], tot[2], tot[3], tile_elem & 0xFu);
-				}
+			for (int i = 0; i < 4; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
+			// AGG payload: packed counts; for the parity paths the tile element (a=1, q)
+			const uint4 agg = PATH == kPathNone ? make_uint4(tot[0], tot[2], tot[3], 0u)
+												: make_uint4(tot[0], tot[2], tot[3], 1u | ((tot[1] & 1u) << 2));
+			if (lane == 0) {
+				sc.tagg[buf] = agg;
 				if (t == 0) {
-					if (lane == 0) {
-						std::uint32_t cs, co, cc;
-						agg_counts<PATH>(agg, init_state, cs, co, cc);
-						const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(tile_elem, init_state);
-						st128_relaxed(&d_incl[0], make_uint4(base0[0] + cs, base0[1] + co, base0[2] + cc,
-															 kDIncl | (epoch << 8) | after));
-					}
+					std::uint32_t cs, co, cc;
+					agg_counts<PATH>(agg, init_state, cs, co, cc);
+					const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, init_state);
+					st128_relaxed(&d_incl[0], make_uint4(base0[0] + cs, base0[1] + co, base0[2] + cc,
+														 kDIncl | (epoch << 8) | after));
 				} else {
+					uint4 d = agg;
+					d.w |= kDAgg | (epoch << 8);
+					st128_relaxed(&d_agg[t], d);
+				}
+			}
+			__syncwarp();
+		};
+		// fold(k): look back over the G-1 tiles before tile k (their AGG words) onto
+		// the INCL word of this CTA's previous tile, publish INCL, post the tile base.
+		auto fold_step = [&](std::uint32_t k) {
+			if (k >= n_mine)
+				return;
+			const std::uint32_t t	= tile_of(k);
+			const int			buf = static_cast<int>(k % kBufs);
+			std::uint32_t		s_t = init_state, base[3] = {base0[0], base0[1], base0[2]};
+			const uint4			agg = sc.tagg[buf];
+			if (!failed && t != 0) {
+				// lane l holds distances j = l*kLB + i (j = 0 is tile t-1)
+				const std::uint32_t W = t < G ? t : G;
+				uint4				lbv[kLB];
+#pragma unroll
+				for (int i = 0; i < kLB; ++i) {
+					const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
+					lbv[i]				  = make_uint4(0, 0, 0, 0);
+					if (j + 1 < W)
+						lbv[i] = ld128_relaxed(&d_agg[t - 1 - j]);
+					else if (j + 1 == W)
+						lbv[i] = ld128_relaxed(&d_incl[t - W]);
+				}
+				bool bad = false;
+#pragma unroll
+				for (int i = 0; i < kLB; ++i) {
+					const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
+					if (j < W && !bad) {
+						const bool			incl_slot = (j + 1 == W);
+						const uint4*		src		  = incl_slot ? &d_incl[t - W] : &d_agg[t - 1 - j];
+						const std::uint32_t want	  = incl_slot ? 2u : 1u;
+						std::uint32_t		spins	  = 0;
+						while (!((lbv[i].w >> 30) == want && ((lbv[i].w >> 8) & 0x3FFFFFu) == epoch)) {
+							if (++spins > kSpinLimit) {
+								record_error(res, kDevErrTimeout);
+								bad = true;
+								break;
+							}
+							if ((spins & 63u) == 0 && aborted(res)) {
+								bad = true;
+								break;
+							}
+							__nanosleep(20);
+							lbv[i] = ld128_relaxed(src);
+						}
+					}
+				}
+				if (__any_sync(kFull, bad)) {
+					failed = true;
+				} else {
+					std::uint32_t s_incl = 0, c_incl[3] = {0, 0, 0};
+#pragma unroll
+					for (int i = 0; i < kLB; ++i)
+						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 == W) {
+							s_incl	  = lbv[i].w & 3u;
+							c_incl[0] = lbv[i].x;
+							c_incl[1] = lbv[i].y;
+							c_incl[2] = lbv[i].z;
+						}
+					const int src_lane = static_cast<int>((W - 1) / kLB);
+					s_incl			   = __shfl_sync(kFull, s_incl, src_lane);
+					c_incl[0]		   = __shfl_sync(kFull, c_incl[0], src_lane);
+					c_incl[1]		   = __shfl_sync(kFull, c_incl[1], src_lane);
+					c_incl[2]		   = __shfl_sync(kFull, c_incl[2], src_lane);
+					std::uint32_t E	   = kIdent;
+#pragma unroll
+					for (int i = kLB - 1; i >= 0; --i)
+						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W)
+							E = compose_fast(E, lbv[i].w & 0xFu);
+					std::uint32_t x = E;
+#pragma unroll
+					for (int off = 1; off < 32; off <<= 1) {
+						const std::uint32_t o = __shfl_down_sync(kFull, x, off);
+						if (lane + off < 32)
+							x = compose_fast(o, x);
+					}
+					std::uint32_t ex = __shfl_down_sync(kFull, x, 1);
+					if (lane == 31)
+						ex = kIdent;
+					std::uint32_t st = PATH == kPathNone ? 0u : apply_fast(ex, s_incl);
+					std::uint32_t cs = 0, co = 0, cc = 0;
+#pragma unroll
+					for (int i = kLB - 1; i >= 0; --i)
+						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W) {
+							std::uint32_t a0, a1, a2;
+							agg_counts<PATH>(lbv[i], st, a0, a1, a2);
+							cs += a0;
+							co += a1;
+							cc += a2;
+							if (PATH != kPathNone)
+								st = apply_fast(lbv[i].w & 0xFu, st);
+						}
+#pragma unroll
+					for (int off = 16; off > 0; off >>= 1) {
+						cs += __shfl_xor_sync(kFull, cs, off);
+						if (BR) {
+							co += __shfl_xor_sync(kFull, co, off);
+							cc += __shfl_xor_sync(kFull, cc, off);
+						}
+					}
+					s_t		= __shfl_sync(kFull, st, 0);
+					base[0] = c_incl[0] + cs;
+					base[1] = c_incl[1] + co;
+					base[2] = c_incl[2] + cc;
 					if (lane == 0) {
-						uint4 d = agg;
-						d.w |= kDAgg | (epoch << 8);
-						st128_relaxed(&d_agg[t], d);
-					}
-					// look-back: lane l holds distances j = l*kLB + i (j = 0 is tile t-1)
-					const std::uint32_t W = t < G ? t : G;
-					uint4				lbv[kLB];
-#pragma unroll
-					for (int i = 0; i < kLB; ++i) {
-						const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
-						lbv[i]				  = make_uint4(0, 0, 0, 0);
-						if (j + 1 < W)
-							lbv[i] = ld128_relaxed(&d_agg[t - 1 - j]);
-						else if (j + 1 == W)
-							lbv[i] = ld128_relaxed(&d_incl[t - W]);
-					}
-					bool bad = false;
-#pragma unroll
-					for (int i = 0; i < kLB; ++i) {
-						const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
-						if (j < W && !bad) {
-							const bool			incl_slot = (j + 1 == W);
-							const uint4*		src = incl_slot ? &d_incl[t - W] : &d_agg[t - 1 - j];
-							const std::uint32_t want = incl_slot ? 2u : 1u;
-							std::uint32_t		spins = 0;
-							while (!((lbv[i].w >> 30) == want && ((lbv[i].w >> 8) & 0x3FFFFFu) == epoch)) {
-								if (++spins > kSpinLimit) {
-									record_error(res, kDevErrTimeout);
-									bad = true;
-									break;
-								}
-								if ((spins & 63u) == 0 && aborted(res)) {
-									bad = true;
-									break;
-								}
-								__nanosleep(20);
-								lbv[i] = ld128_relaxed(src);
-							}
-						}
-					}
-					if (__any_sync(kFull, bad)) {
-						failed = true;
-					} else {
-						std::uint32_t s_incl = 0, c_incl[3] = {0, 0, 0};
-#pragma unroll
-						for (int i = 0; i < kLB; ++i)
-							if (static_cast<std::uint32_t>(lane) * kLB + i + 1 == W) {
-								s_incl	  = lbv[i].w & 3u;
-								c_incl[0] = lbv[i].x;
-								c_incl[1] = lbv[i].y;
-								c_incl[2] = lbv[i].z;
-							}
-						const int src_lane = static_cast<int>((W - 1) / kLB);
-						s_incl			   = __shfl_sync(kFull, s_incl, src_lane);
-						c_incl[0]		   = __shfl_sync(kFull, c_incl[0], src_lane);
-						c_incl[1]		   = __shfl_sync(kFull, c_incl[1], src_lane);
-						c_incl[2]		   = __shfl_sync(kFull, c_incl[2], src_lane);
-						std::uint32_t E	   = kIdent;
-#pragma unroll
-						for (int i = kLB - 1; i >= 0; --i)
-							if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W)
-								E = compose_fast(E, lbv[i].w & 0xFu);
-						std::uint32_t x = E;
-#pragma unroll
-						for (int off = 1; off < 32; off <<= 1) {
-							const std::uint32_t o = __shfl_down_sync(kFull, x, off);
-							if (lane + off < 32)
-								x = compose_fast(o, x);
-						}
-						std::uint32_t ex = __shfl_down_sync(kFull, x, 1);
-						if (lane == 31)
-							ex = kIdent;
-						std::uint32_t st = PATH == kPathNone ? 0u : apply_fast(ex, s_incl);
-						std::uint32_t cs = 0, co = 0, cc = 0;
-#pragma unroll
-						for (int i = kLB - 1; i >= 0; --i)
-							if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W) {
-								std::uint32_t a0, a1, a2;
-								agg_counts<PATH>(lbv[i], st, a0, a1, a2);
-								cs += a0;
-								co += a1;
-								cc += a2;
-								if (PATH != kPathNone)
-									st = apply_fast(lbv[i].w & 0xFu, st);
-							}
-#pragma unroll
-						for (int off = 16; off > 0; off >>= 1) {
-							cs += __shfl_xor_sync(kFull, cs, off);
-							if (BR) {
-								co += __shfl_xor_sync(kFull, co, off);
-								cc += __shfl_xor_sync(kFull, cc, off);
-							}
-						}
-						s_t		= __shfl_sync(kFull, st, 0);
-						base[0] = c_incl[0] + cs;
-						base[1] = c_incl[1] + co;
-						base[2] = c_incl[2] + cc;
-						if (lane == 0) {
-							std::uint32_t c0, c1, c2;
-							agg_counts<PATH>(agg, s_t, c0, c1, c2);
-							const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(tile_elem, s_t);
-							st128_relaxed(&d_incl[t], make_uint4(base[0] + c0, base[1] + c1, base[2] + c2,
-																 kDIncl | (epoch << 8) | after));
-						}
+						std::uint32_t c0, c1, c2;
+						agg_counts<PATH>(agg, s_t, c0, c1, c2);
+						const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, s_t);
+						st128_relaxed(&d_incl[t], make_uint4(base[0] + c0, base[1] + c1, base[2] + c2,
+															 kDIncl | (epoch << 8) | after));
 					}
 				}
 			}
@@ -402,11 +396,14 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			__syncwarp();
 			if (lane == 0)
 				mbar_arrive(&base_bar[buf]);
+		};
+		// The workers publish tile k+1's totals long before they need tile k's base,
+		// so AGG words are out well ahead of every other CTA's fold.
+		agg_step(0);
+		for (std::uint32_t k = 0; k < n_mine; ++k) {
+			agg_step(k + 1);
+			fold_step(k);
 		}
-		// drain: every issued copy must land before the CTA exits
-		if (lane == 0)
-			for (std::uint32_t k = (issued > 2 ? issued - 2 : 0); k < issued; ++k)
-				mbar_wait(&full_bar[k & 1], (k >> 1) & 1u, res);
 	} else {
 		// ================================================================ workers ====
 		const std::uint32_t wtid	 = static_cast<std::uint32_t>(tid);	 // 0..511
@@ -424,10 +421,49 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 		const std::uint32_t cap_s = a.cap_s > 0xFFFFFFFFull ? 0xFFFFFFFFu : static_cast<std::uint32_t>(a.cap_s);
 		const std::uint32_t cap_b = a.cap_b > 0xFFFFFFFFull ? 0xFFFFFFFFu : static_cast<std::uint32_t>(a.cap_b);
 
+		// ring refills are issued by lane 0 of worker warp 0
+		std::uint32_t issued = 0;
+		auto issue = [&](std::uint32_t k) {
+			if (k >= n_mine)
+				return;
+			issued		  = k + 1;
+			const int s	  = static_cast<int>(k & 1);
+			const unsigned long long row0 = static_cast<unsigned long long>(tile_of(k)) * kWsRows;
+			if (row0 >= wa.rows_full) {
+				// nothing of this tile is in the tensor: its workers read the tail bytes
+				// from global memory themselves
+				mbar_arrive(&full_bar[s]);
+			} else {
+				// rows past the tensor's end come back as zeros (and count as delivered)
+				mbar_arrive_expect_tx(&full_bar[s], kWsTile);
+				tma_rows(ring + s * kWsTile, &tmap, static_cast<int>(row0), &full_bar[s]);
+			}
+		};
+		if (warp == 0 && lane == 0) {
+			if (wa.rows_full)
+				asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<std::uint64_t>(&tmap)) : "memory");
+			issue(0);
+			issue(1);
+		}
+
+		// bytes of word h of this thread that belong to the document (or chunk)
+		auto valid_mask = [&](unsigned long long qw, bool interior) -> std::uint32_t {
+			if (interior)
+				return 0xFFFFFFFFu;
+			int lo = 0, hi = 32;
+			if (qw < a.o)
+				lo = (a.o - qw) > 32 ? 32 : static_cast<int>(a.o - qw);
+			if (doc_end < qw + 32)
+				hi = doc_end <= qw ? 0 : static_cast<int>(doc_end - qw);
+			if (hi < lo)
+				hi = lo;
+			return bit_range(lo, hi);
+		};
+
 		auto phase_a = [&](std::uint32_t k, WsFront& F) -> bool {
 			const std::uint32_t t	= tile_of(k);
 			const int			s	= static_cast<int>(k & 1);
-			const int			buf = s;
+			const int			buf = static_cast<int>(k % kBufs);
 			if (!mbar_wait(&full_bar[s], (k >> 1) & 1u, res)) {
 				sc.failed = 1;
 				return false;
@@ -452,22 +488,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				if (lane == 0 && !first)
 					pdelim = a.base[q0 - 1] == delim ? 1u : 0u;
 			}
+			std::uint32_t ex0[2];
 #pragma unroll
 			for (int h = 0; h < 2; ++h) {
-				const unsigned long long qw = q0 + 32u * h;
-				std::uint32_t			 vm = 0xFFFFFFFFu;
-				int						 lo = 0, hi = 32;
-				if (!interior) {
-					if (qw < a.o)
-						lo = (a.o - qw) > 32 ? 32 : static_cast<int>(a.o - qw);
-					if (doc_end < qw + 32)
-						hi = doc_end <= qw ? 0 : static_cast<int>(doc_end - qw);
-					if (hi < lo)
-						hi = lo;
-					vm = bit_range(lo, hi);
-				}
-				F.vm[h] = vm;
-				std::uint32_t r[8];
+				const std::uint32_t vm = valid_mask(q0 + 32u * h, interior);
+				std::uint32_t		r[8];
 				{
 					const uint4 x = *reinterpret_cast<const uint4*>(stage + chunk_off[2 * h]);
 					const uint4 y = *reinterpret_cast<const uint4*>(stage + chunk_off[2 * h + 1]);
@@ -494,16 +519,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				F.D[h] = D;
 				std::uint32_t e[4];
 				if (PATH == kPathNone) {
-					F.ex0[h] = F.dd[h] = 0;
-					e[0]			   = __popc(S);
-					e[1]			   = 0;
-					e[2]			   = BR ? __popc(O) : 0u;
-					e[3]			   = BR ? __popc(C) : 0u;
+					ex0[h] = 0;
+					e[0]   = __popc(S);
+					e[1]   = 0;
+					e[2]   = BR ? __popc(O) : 0u;
+					e[3]   = BR ? __popc(C) : 0u;
 				} else {
-					F.ex0[h] = prefix_xor32(D) ^ D;
-					F.dd[h]	 = 0;  // doubled path: completed once both words are known
-					e[0]	 = 0;
-					e[1]	 = __popc(D) & 1u;
+					ex0[h] = prefix_xor32(D) ^ D;
+					e[0]   = 0;
+					e[1]   = __popc(D) & 1u;
 					e[2] = e[3] = 0;
 				}
 				if (h == 0)
@@ -513,12 +537,12 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
 					for (int i = 0; i < 4; ++i) v[i] = e[i];
 			}
+			F.dd[0] = F.dd[1] = 0;
 			if (PATH == kPathParity || PATH == kPathDoubled) {
-				std::uint32_t dd0 = 0, dd1 = 0;
 				if (PATH == kPathDoubled) {
 					// previous-byte-delimiter bits: word 1 takes word 0's last byte; word 0
 					// takes the previous thread's last byte (lane - 1, or memory for lane 0)
-					std::uint32_t prev = __shfl_up_sync(kFull, F.D[1] >> 31, 1);
+					std::uint32_t prev	= __shfl_up_sync(kFull, F.D[1] >> 31, 1);
 					const bool	  first = (q0 <= a.o);
 					if (lane == 0)
 						prev = pdelim;
@@ -527,23 +551,21 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 						const int lo0 = static_cast<int>(a.o - q0);	 // 0..63
 						prev		  = a.carry_in ? (a.carry_in->last_delim & 1u) : 0u;
 						if (lo0 < 32) {
-							dd0 = F.D[0] & ((F.D[0] << 1) | (prev << lo0));
-							dd1 = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
+							F.dd[0] = F.D[0] & ((F.D[0] << 1) | (prev << lo0));
+							F.dd[1] = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
 						} else {
-							dd0 = 0;
-							dd1 = F.D[1] & ((F.D[1] << 1) | (prev << (lo0 - 32)));
+							F.dd[0] = 0;
+							F.dd[1] = F.D[1] & ((F.D[1] << 1) | (prev << (lo0 - 32)));
 						}
 					} else {
-						dd0 = F.D[0] & ((F.D[0] << 1) | (prev & 1u));
-						dd1 = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
+						F.dd[0] = F.D[0] & ((F.D[0] << 1) | (prev & 1u));
+						F.dd[1] = F.D[1] & ((F.D[1] << 1) | (F.D[0] >> 31));
 					}
 				}
-				F.dd[0] = dd0;
-				F.dd[1] = dd1;
 				// counts of each word under both parity hypotheses
 #pragma unroll
 				for (int h = 0; h < 2; ++h) {
-					const std::uint32_t m0 = F.ex0[h] | F.dd[h], m1 = ~F.ex0[h] | F.dd[h];
+					const std::uint32_t m0 = ex0[h] | F.dd[h], m1 = ~ex0[h] | F.dd[h];
 					std::uint32_t*		e  = h == 0 ? w0 : v;
 					e[0] = __popc(F.S[h] & ~m0) | (__popc(F.S[h] & ~m1) << 16);
 					if (BR) {
@@ -555,8 +577,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			} else {
 				OpSum3()(w0, v);
 			}
-#pragma unroll
-			for (int i = 0; i < 4; ++i) F.w0[i] = w0[i];
 			if (PATH == kPathNone)
 				warp_scan(v, OpSum3(), lane, 32);
 			else
@@ -572,13 +592,23 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			__syncwarp();
 			if (lane == 0)
 				mbar_arrive(&tot_bar[buf]);
+			if (warp == 0) {
+				// once every worker has classified tile k, its slot takes tile k+2
+				if (!mbar_wait(&tot_bar[buf], (k / kBufs) & 1u, res)) {
+					sc.failed = 1;
+					return false;
+				}
+				if (lane == 0)
+					issue(k + 2);
+				__syncwarp();
+			}
 			return true;
 		};
 
 		auto phase_b = [&](std::uint32_t k, const WsFront& F) -> bool {
 			const std::uint32_t t	= tile_of(k);
-			const int			buf = static_cast<int>(k & 1);
-			if (!mbar_wait(&base_bar[buf], (k >> 1) & 1u, res) || sc.failed) {
+			const int			buf = static_cast<int>(k % kBufs);
+			if (!mbar_wait(&base_bar[buf], (k / kBufs) & 1u, res) || sc.failed) {
 				sc.failed = 1;
 				return false;
 			}
@@ -589,42 +619,39 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
 			for (int i = 0; i < 4; ++i) pre[i] = sc.wpre[buf][warp][i];
 			const std::uint32_t base[3] = {sc.base[buf][0], sc.base[buf][1], sc.base[buf][2]};
-			// prefixes of word 0 and word 1
+			// prefix of word 0: the warp's prefix, then this thread's warp-exclusive prefix
 			std::uint32_t p0[4] = {F.ex[0], F.ex[1], F.ex[2], F.ex[3]};
 			if (PATH == kPathNone)
 				OpSum3()(pre, p0);
 			else
 				OpParity()(pre, p0);
-			std::uint32_t p1[4] = {F.w0[0], F.w0[1], F.w0[2], F.w0[3]};
-			std::uint32_t p0c[4] = {p0[0], p0[1], p0[2], p0[3]};
-			if (PATH == kPathNone)
-				OpSum3()(p0c, p1);
-			else
-				OpParity()(p0c, p1);
+			std::uint32_t off[3], p_w = 0;
+			if (PATH == kPathNone) {
+				off[0] = p0[0];
+				off[1] = p0[2];
+				off[2] = p0[3];
+			} else {
+				p_w	   = p_t ^ (p0[1] & 1u);
+				off[0] = half16(p0[0], p_t);
+				off[1] = half16(p0[2], p_t);
+				off[2] = half16(p0[3], p_t);
+			}
+			const bool interior = static_cast<unsigned long long>(t) * kWsTile >= a.o
+							   && static_cast<unsigned long long>(t + 1) * kWsTile <= doc_end;
 #pragma unroll
 			for (int h = 0; h < 2; ++h) {
-				const std::uint32_t* pw = h == 0 ? p0 : p1;
 				const unsigned long long qw = q0 + 32u * h;
-				const std::uint32_t	 vm	= F.vm[h];
-				std::uint32_t		 off[3], p_w = 0;
-				if (PATH == kPathNone) {
-					off[0] = pw[0];
-					off[1] = pw[2];
-					off[2] = pw[3];
-				} else {
-					p_w	   = p_t ^ pw[1];
-					off[0] = half16(pw[0], p_t);
-					off[1] = half16(pw[2], p_t);
-					off[2] = half16(pw[3], p_t);
+				const std::uint32_t		 vm = valid_mask(qw, interior);
+				std::uint32_t			 mask = 0;
+				if (PATH != kPathNone) {
+					const std::uint32_t ex0 = prefix_xor32(F.D[h]) ^ F.D[h];
+					mask = ((ex0 ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd[h]) & vm;
 				}
-				std::uint32_t mask = 0;
-				if (PATH != kPathNone)
-					mask = ((F.ex0[h] ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd[h]) & vm;
 				if (vm != 0 && doc_end <= qw + 32 && doc_end > qw) {
 					const int			hi		  = static_cast<int>(doc_end - qw);
 					const std::uint32_t elem	  = 1u | ((__popc(F.D[h]) & 1u) << 2);
 					const std::uint32_t endstate  = PATH == kPathNone ? 0u : apply_fast(elem, p_w << 1);
-					const std::uint32_t last_flag = (F.D[h] >> (hi - 1)) & 1u;
+					const std::uint32_t last_flag = PATH == kPathNone ? 0u : (F.D[h] >> (hi - 1)) & 1u;
 					const std::uint32_t unclosed  = PATH == kPathNone ? 0u : (((endstate >> 1) & 1u) | last_flag);
 					res->unclosed				  = unclosed;
 					if (a.carry_out) {
@@ -636,8 +663,20 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				}
 				std::uint32_t		m	 = F.S[h] & ~mask;
 				std::uint32_t		si	 = base[0] + off[0];
+				const std::uint32_t no0	 = base[1] + off[1];
+				const std::uint32_t nc0	 = base[2] + off[2];
 				const std::uint32_t pos0 = byte_base + static_cast<std::uint32_t>(qw - a.o);
 				const unsigned char* gb	 = a.base + qw;	 // input bytes (global, L2-resident)
+				if (h == 0) {
+					// word 1 starts after word 0's selected bytes and toggles
+					off[0] += __popc(m);
+					if (BR) {
+						off[1] += __popc(F.O[0] & ~mask);
+						off[2] += __popc(F.C[0] & ~mask);
+					}
+					if (PATH != kPathNone)
+						p_w ^= __popc(F.D[0]) & 1u;
+				}
 				if (!BR) {
 					if (si + static_cast<std::uint32_t>(__popc(m)) <= cap_s && !want_chars && !want_pairs) {
 						std::uint32_t* out = a.pos + si;
@@ -663,8 +702,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				} else {
 					const std::uint32_t selo = F.O[h] & ~mask;
 					const std::uint32_t selc = F.C[h] & ~mask;
-					const std::uint32_t no0	 = base[1] + off[1];
-					const std::uint32_t nc0	 = base[2] + off[2];
 					std::uint32_t		bi	 = no0 + nc0;
 					long long			dep	 = static_cast<long long>(no0) - static_cast<long long>(nc0);
 					const std::uint32_t bm	 = selo | selc;
@@ -709,20 +746,31 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			return true;
 		};
 
-		WsFront f0, f1;
-		bool	ok = n_mine > 0 ? phase_a(0, f0) : true;
-		for (std::uint32_t k = 0; ok && k < n_mine; k += 2) {
-			if (k + 1 < n_mine)
-				ok = phase_a(k + 1, f1);
-			if (!ok || !phase_b(k, f0))
-				break;
-			if (k + 1 >= n_mine)
-				break;
-			if (k + 2 < n_mine)
-				ok = phase_a(k + 2, f0);
-			if (!ok || !phase_b(k + 1, f1))
-				break;
-		}
+		// A runs kAhead tiles ahead of B; the four fronts rotate through static names
+		// so they stay in registers.
+		static_assert(kAhead == 3 && kBufs == 4, "the rotation below is written for 3 + 1 fronts");
+		WsFront f0, f1, f2, f3;
+		auto step = [&](std::uint32_t k, WsFront& Fa, WsFront& Fb) -> bool {
+			if (k >= n_mine)
+				return false;
+			if (k + kAhead < n_mine && !phase_a(k + kAhead, Fa))
+				return false;
+			return phase_b(k, Fb);
+		};
+		bool ok = true;
+		if (n_mine > 0)
+			ok = phase_a(0, f0);
+		if (ok && n_mine > 1)
+			ok = phase_a(1, f1);
+		if (ok && n_mine > 2)
+			ok = phase_a(2, f2);
+		for (std::uint32_t k = 0; ok && k < n_mine; k += kBufs)
+			ok = step(k, f3, f0) && step(k + 1, f0, f1) && step(k + 2, f1, f2) && step(k + 3, f2, f3);
+
+		// drain: every issued copy must land before the CTA exits
+		if (warp == 0 && lane == 0)
+			for (std::uint32_t k = (issued > 2 ? issued - 2 : 0); k < issued; ++k)
+				mbar_wait(&full_bar[k & 1], (k >> 1) & 1u, res);
 	}
 	__syncthreads();
 
