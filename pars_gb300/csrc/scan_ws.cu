@@ -120,7 +120,9 @@ struct OpSum3 {
 	}
 };
 
-template<class Op>
+// Inclusive warp scan of 4-lane elements; only the first NL lanes are live (the
+// others are zero on every thread, which the compiler then folds away).
+template<int NL, class Op>
 __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane, int n_active) {
 #pragma unroll
 	for (int off = 1; off < 32; off <<= 1) {
@@ -128,7 +130,7 @@ __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane
 			break;
 		std::uint32_t y[4];
 #pragma unroll
-		for (int i = 0; i < 4; ++i) y[i] = __shfl_up_sync(kFull, x[i], off);
+		for (int i = 0; i < 4; ++i) y[i] = i < NL ? __shfl_up_sync(kFull, x[i], off) : 0u;
 		if (lane >= off)
 			op(y, x);
 	}
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	unsigned char*		ring	= smem + (tbl_win - win0) + SmemWs::kTblBytes;
 
 	const int			tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	constexpr int		NL	= BR ? 4 : 2;  // live element lanes: S counts, parity (, O, C)
 	const DevPlan*		P	= a.plan;
 	DevResult*			res = a.res;
 	uint4*				d_agg  = static_cast<uint4*>(a.tiles);
@@ -219,23 +222,23 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			std::uint32_t w[4] = {0, 0, 0, 0};
 			if (lane < kWorkers)
 #pragma unroll
-				for (int i = 0; i < 4; ++i) w[i] = sc.wtot[buf][lane][i];
+				for (int i = 0; i < NL; ++i) w[i] = sc.wtot[buf][lane][i];
 			if (PATH == kPathNone)
-				warp_scan(w, OpSum3(), lane, kWorkers);
+				warp_scan<NL>(w, OpSum3(), lane, kWorkers);
 			else
-				warp_scan(w, OpParity(), lane, kWorkers);
-			std::uint32_t we[4];
+				warp_scan<NL>(w, OpParity(), lane, kWorkers);
+			std::uint32_t we[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < 4; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
+			for (int i = 0; i < NL; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
 			if (lane == 0)
 #pragma unroll
 				for (int i = 0; i < 4; ++i) we[i] = 0;
 			if (lane < kWorkers)
 #pragma unroll
-				for (int i = 0; i < 4; ++i) sc.wpre[buf][lane][i] = we[i];
-			std::uint32_t tot[4];
+				for (int i = 0; i < NL; ++i) sc.wpre[buf][lane][i] = we[i];
+			std::uint32_t tot[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < 4; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
+			for (int i = 0; i < NL; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
 			// AGG payload: packed counts; for the parity paths the tile element (a=1, q)
 			const uint4 agg = PATH == kPathNone ? make_uint4(tot[0], tot[2], tot[3], 0u)
 												: make_uint4(tot[0], tot[2], tot[3], 1u | ((tot[1] & 1u) << 2));
@@ -577,18 +580,20 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			} else {
 				OpSum3()(w0, v);
 			}
+			if (!BR)
+				v[2] = v[3] = 0;
 			if (PATH == kPathNone)
-				warp_scan(v, OpSum3(), lane, 32);
+				warp_scan<NL>(v, OpSum3(), lane, 32);
 			else
-				warp_scan(v, OpParity(), lane, 32);
+				warp_scan<NL>(v, OpParity(), lane, 32);
 #pragma unroll
 			for (int i = 0; i < 4; ++i) {
-				const std::uint32_t e = __shfl_up_sync(kFull, v[i], 1);
+				const std::uint32_t e = i < NL ? __shfl_up_sync(kFull, v[i], 1) : 0u;
 				F.ex[i]				  = lane == 0 ? 0u : e;
 			}
 			if (lane == 31)
 #pragma unroll
-				for (int i = 0; i < 4; ++i) sc.wtot[buf][warp][i] = v[i];
+				for (int i = 0; i < NL; ++i) sc.wtot[buf][warp][i] = v[i];
 			__syncwarp();
 			if (lane == 0)
 				mbar_arrive(&tot_bar[buf]);
@@ -615,9 +620,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			const unsigned long long q0	 = static_cast<unsigned long long>(t) * kWsTile + 64u * wtid;
 			const std::uint32_t		 s_t = sc.state[buf];
 			const std::uint32_t		 p_t = (s_t >> 1) & 1u;
-			std::uint32_t			 pre[4];
+			std::uint32_t			 pre[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < 4; ++i) pre[i] = sc.wpre[buf][warp][i];
+			for (int i = 0; i < NL; ++i) pre[i] = sc.wpre[buf][warp][i];
 			const std::uint32_t base[3] = {sc.base[buf][0], sc.base[buf][1], sc.base[buf][2]};
 			// prefix of word 0: the warp's prefix, then this thread's warp-exclusive prefix
 			std::uint32_t p0[4] = {F.ex[0], F.ex[1], F.ex[2], F.ex[3]};
@@ -746,26 +751,21 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			return true;
 		};
 
-		// A runs kAhead tiles ahead of B; the four fronts rotate through static names
-		// so they stay in registers.
+		// A runs kAhead tiles ahead of B.  The fronts rotate by register moves, which
+		// keeps a single copy of each phase in the loop (an unrolled rotation
+		// multiplies the code and misses in the instruction cache).
 		static_assert(kAhead == 3 && kBufs == 4, "the rotation below is written for 3 + 1 fronts");
 		WsFront f0, f1, f2, f3;
-		auto step = [&](std::uint32_t k, WsFront& Fa, WsFront& Fb) -> bool {
-			if (k >= n_mine)
-				return false;
-			if (k + kAhead < n_mine && !phase_a(k + kAhead, Fa))
-				return false;
-			return phase_b(k, Fb);
-		};
-		bool ok = true;
-		if (n_mine > 0)
-			ok = phase_a(0, f0);
-		if (ok && n_mine > 1)
-			ok = phase_a(1, f1);
-		if (ok && n_mine > 2)
-			ok = phase_a(2, f2);
-		for (std::uint32_t k = 0; ok && k < n_mine; k += kBufs)
-			ok = step(k, f3, f0) && step(k + 1, f0, f1) && step(k + 2, f1, f2) && step(k + 3, f2, f3);
+		for (long long kk = -kAhead; kk < static_cast<long long>(n_mine); ++kk) {
+			const std::uint32_t ka = static_cast<std::uint32_t>(kk + kAhead);
+			if (ka < n_mine && !phase_a(ka, f3))
+				break;
+			if (kk >= 0 && !phase_b(static_cast<std::uint32_t>(kk), f0))
+				break;
+			f0 = f1;
+			f1 = f2;
+			f2 = f3;
+		}
 
 		// drain: every issued copy must land before the CTA exits
 		if (warp == 0 && lane == 0)
