@@ -436,8 +436,12 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	const size_t tdesc = fast ? 2 * sizeof(uint4) : sizeof(TileDescG);  // fast: AGG + INCL words
 	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
 		return r;
+	// The bracket-less warp-specialised kernels keep no per-byte toggle planes, so a
+	// scan that wants the masked bitmap runs the bracket variant (with no brackets
+	// in the plan its bracket planes are empty).
+	const bool br_kernel = pl->host.has_brackets != 0 || (use_ws(s.path) && (s.flags & PARS_WANT_MASK));
 	if (fast) {
-		if (int r = ensure_fast_config(ctx, s.path, pl->host.has_brackets != 0))
+		if (int r = ensure_fast_config(ctx, s.path, br_kernel))
 			return r;
 	} else {
 		if (int r = ensure_scan_config(ctx, s.path))
@@ -472,7 +476,7 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	a.flags		= s.flags;
 	void* args[] = {&a};
 	if (fast && use_ws(s.path)) {
-		const bool	br	 = pl->host.has_brackets != 0;
+		const bool	br	 = br_kernel;
 		const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
 		WsArgs		wa {a, total / 128};
 		CUtensorMap map;

@@ -23,15 +23,26 @@
 //            order A(0), A(1), A(2), then A(k+3), B(k) for k = 0, 1, ...: the
 //            class planes of four tiles live in registers, so a tile's totals are
 //            published three tiles before its base is needed.
-//   manager  agg(k):  wait TOT[k%4] -> scan the 16 warp totals -> publish AGG.
-//            fold(k): fold the look-back -> publish INCL -> post the tile base;
-//                     arrive BASE[k%4].  Order agg(0), then agg(k+1), fold(k).
+//   manager  agg(k):  wait TOT[k%4] -> scan the 16 warp totals -> publish the tile's
+//                     AGG word (counts under both in-string hypotheses, parity).
+//            fold(k): reduce the AGG words of the G-1 tiles since this CTA's
+//                     previous tile, combine with the CTA's own running prefix,
+//                     post the tile base; arrive BASE[k%4].  Order agg(0), then
+//                     agg(k+1), fold(k).
+//
+// There are no inclusive-prefix words: each CTA carries the prefix of its own
+// tiles, so a fold waits only for other CTAs' aggregates, never for their prefix
+// (a chain of prefixes would advance G tiles per fold latency).
 //
 // Running A ahead matters because the CTAs of one wave drift apart by several
 // tile times: with A and B in lock step, each fold waited for the slowest
 // predecessor in its wave.
 //
-// Look-back words and their fold are shared with scan_fast.cu (fast_common.cuh).
+// A tile's aggregate is published as one 64-bit word per count plane (structurals;
+// opens and closes for bracket plans): the packed counts in the low half, the
+// scan's epoch, the tile's toggle parity and a valid bit in the high half.  64 bits
+// is the widest access the memory model makes single-copy atomic, so each word
+// validates itself; a 128-bit word can be observed half old, half new.
 // Reference semantics: include/pars/model/scan.hpp:33-72 and nest.hpp:55-76.
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -95,8 +106,14 @@ struct WsScratch {
 // planes, the doubled path's "previous byte was a delimiter" bits, and the
 // warp-exclusive prefix of the thread.  Everything else is recomputed in B.
 struct WsFront {
-	std::uint32_t S[2], D[2], dd[2];
-	std::uint32_t O[2], C[2];  // bracket planes (unused without brackets)
+	// bracket kernels: the class planes of both words (masked to the document) and
+	// the doubled path's "previous byte was a delimiter" bits
+	std::uint32_t S[2], D[2], dd[2], O[2], C[2];
+	// bracket-less kernels: each word's selected structurals if the word starts
+	// outside (sel0) or inside (sel1) a string; B only has to pick one
+	std::uint32_t sel0[2], sel1[2];
+	// warp-exclusive prefix; bracket-less kernels keep word 0's toggle parity in
+	// bit 1 of ex[1]
 	std::uint32_t ex[4];
 };
 
@@ -122,6 +139,69 @@ struct OpSum3 {
 
 // Inclusive warp scan of 4-lane elements; only the first NL lanes are live (the
 // others are zero on every thread, which the compiler then folds away).
+// Tag half of a tile's aggregate words: this scan's epoch (22 bits), the tile's
+// toggle parity q and a valid bit.  The epoch is never 0, so a cleared or stale
+// word never matches.
+__device__ __forceinline__ std::uint32_t agg_tag(std::uint32_t epoch, std::uint32_t q) {
+	return (epoch << 8) | (q << 1) | 1u;
+}
+
+__device__ __forceinline__ bool agg_valid(std::uint64_t w, std::uint32_t epoch) {
+	return static_cast<std::uint32_t>(w >> 40) == epoch && ((w >> 32) & 1u);
+}
+
+// Aggregate of a run of tiles for the bracket-less and parity paths: counts of
+// structurals (c[0], c[1]), opens (c[2], c[3]) and closes (c[4], c[5]) when the run
+// is entered outside / inside a string, and the run's toggle parity q.  (The no-
+// string path keeps plain sums in c[0], c[2], c[4].)  Counts are 32-bit: a window
+// of up to G - 1 tiles overflows the 16-bit halves of a single tile's word.
+struct WinElem {
+	std::uint32_t c[6] = {0, 0, 0, 0, 0, 0};
+	std::uint32_t q	   = 0;
+
+	template<int PATH, bool BR>
+	__device__ static WinElem of(const std::uint64_t (&v)[BR ? 3 : 1]) {
+		WinElem e;
+#pragma unroll
+		for (int c = 0; c < (BR ? 3 : 1); ++c) {
+			const std::uint32_t x = static_cast<std::uint32_t>(v[c]);
+			e.c[2 * c]			  = PATH == kPathNone ? x : (x & 0xFFFFu);
+			e.c[2 * c + 1]		  = PATH == kPathNone ? x : (x >> 16);
+		}
+		e.q = PATH == kPathNone ? 0u : static_cast<std::uint32_t>(v[0] >> 33) & 1u;
+		return e;
+	}
+	// this run followed by `b`
+	__device__ WinElem then(const WinElem& b) const {
+		WinElem r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i) {
+			r.c[2 * i]	   = c[2 * i] + (q ? b.c[2 * i + 1] : b.c[2 * i]);
+			r.c[2 * i + 1] = c[2 * i + 1] + (q ? b.c[2 * i] : b.c[2 * i + 1]);
+		}
+		r.q = q ^ b.q;
+		return r;
+	}
+	template<bool BR>
+	__device__ WinElem shfl_down(int off) const {
+		WinElem r;
+		const int n = BR ? 6 : 2;
+#pragma unroll
+		for (int i = 0; i < 6; ++i) r.c[i] = i < n ? __shfl_down_sync(kFull, c[i], off) : 0u;
+		r.q = __shfl_down_sync(kFull, q, off);
+		return r;
+	}
+	template<bool BR>
+	__device__ WinElem shfl0() const {
+		WinElem r;
+		const int n = BR ? 6 : 2;
+#pragma unroll
+		for (int i = 0; i < 6; ++i) r.c[i] = i < n ? __shfl_sync(kFull, c[i], 0) : 0u;
+		r.q = __shfl_sync(kFull, q, 0);
+		return r;
+	}
+};
+
 template<int NL, class Op>
 __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane, int n_active) {
 #pragma unroll
@@ -162,8 +242,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	constexpr int		NL	= BR ? 4 : 2;  // live element lanes: S counts, parity (, O, C)
 	const DevPlan*		P	= a.plan;
 	DevResult*			res = a.res;
-	uint4*				d_agg  = static_cast<uint4*>(a.tiles);
-	uint4*				d_incl = d_agg + a.ntiles;
+	std::uint64_t*		d_agg  = static_cast<std::uint64_t*>(a.tiles);	// [3][ntiles]
 	const std::uint32_t G	   = gridDim.x;
 	const std::uint32_t epoch  = a.epoch & 0x3FFFFFu;
 	const std::uint32_t ntiles = static_cast<std::uint32_t>(a.ntiles);
@@ -244,130 +323,94 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 												: make_uint4(tot[0], tot[2], tot[3], 1u | ((tot[1] & 1u) << 2));
 			if (lane == 0) {
 				sc.tagg[buf] = agg;
-				if (t == 0) {
-					std::uint32_t cs, co, cc;
-					agg_counts<PATH>(agg, init_state, cs, co, cc);
-					const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, init_state);
-					st128_relaxed(&d_incl[0], make_uint4(base0[0] + cs, base0[1] + co, base0[2] + cc,
-														 kDIncl | (epoch << 8) | after));
-				} else {
-					uint4 d = agg;
-					d.w |= kDAgg | (epoch << 8);
-					st128_relaxed(&d_agg[t], d);
+				// one self-validating 64-bit word per count plane: a reader that sees
+				// this scan's tag sees the payload stored with it
+				const std::uint64_t tag = static_cast<std::uint64_t>(agg_tag(epoch, (agg.w >> 2) & 1u)) << 32;
+				st_relaxed64(&d_agg[t], tag | agg.x);
+				if (BR) {
+					st_relaxed64(&d_agg[ntiles + t], tag | agg.y);
+					st_relaxed64(&d_agg[2ull * ntiles + t], tag | agg.z);
 				}
 			}
 			__syncwarp();
 		};
-		// fold(k): look back over the G-1 tiles before tile k (their AGG words) onto
-		// the INCL word of this CTA's previous tile, publish INCL, post the tile base.
+		// Running prefix of this CTA's own tiles: the state and counts after its
+		// previous tile (before its first tile: the document's initial values).
+		std::uint32_t s_prev = init_state, base_prev[3] = {base0[0], base0[1], base0[2]};
+		// fold(k): reduce the AGG words of the tiles between this CTA's previous tile
+		// and tile t (at most G - 1 words, all from other CTAs), combine them with the
+		// running prefix, post the tile base.  No CTA waits for another's prefix: only
+		// for its aggregates, which the workers publish tiles ahead.
 		auto fold_step = [&](std::uint32_t k) {
 			if (k >= n_mine)
 				return;
-			const std::uint32_t t	= tile_of(k);
-			const int			buf = static_cast<int>(k % kBufs);
-			std::uint32_t		s_t = init_state, base[3] = {base0[0], base0[1], base0[2]};
-			const uint4			agg = sc.tagg[buf];
-			if (!failed && t != 0) {
-				// lane l holds distances j = l*kLB + i (j = 0 is tile t-1)
-				const std::uint32_t W = t < G ? t : G;
-				uint4				lbv[kLB];
+			const std::uint32_t t	 = tile_of(k);
+			const int			buf	 = static_cast<int>(k % kBufs);
+			const uint4			agg	 = sc.tagg[buf];
+			std::uint32_t		s_t	 = s_prev, base[3] = {base_prev[0], base_prev[1], base_prev[2]};
+			if (!failed) {
+				const std::uint32_t nwin = k == 0 ? t : G - 1;
+				constexpr int		NP	 = BR ? 3 : 1;	// count planes
+				std::uint64_t		lbv[kLB][NP];
 #pragma unroll
 				for (int i = 0; i < kLB; ++i) {
 					const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
-					lbv[i]				  = make_uint4(0, 0, 0, 0);
-					if (j + 1 < W)
-						lbv[i] = ld128_relaxed(&d_agg[t - 1 - j]);
-					else if (j + 1 == W)
-						lbv[i] = ld128_relaxed(&d_incl[t - W]);
+#pragma unroll
+					for (int c = 0; c < NP; ++c)
+						lbv[i][c] = j < nwin ? ld_relaxed64(&d_agg[c * static_cast<std::uint64_t>(ntiles) + t - 1 - j]) : 0ull;
 				}
 				bool bad = false;
 #pragma unroll
 				for (int i = 0; i < kLB; ++i) {
 					const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
-					if (j < W && !bad) {
-						const bool			incl_slot = (j + 1 == W);
-						const uint4*		src		  = incl_slot ? &d_incl[t - W] : &d_agg[t - 1 - j];
-						const std::uint32_t want	  = incl_slot ? 2u : 1u;
-						std::uint32_t		spins	  = 0;
-						while (!((lbv[i].w >> 30) == want && ((lbv[i].w >> 8) & 0x3FFFFFu) == epoch)) {
-							if (++spins > kSpinLimit) {
-								record_error(res, kDevErrTimeout);
-								bad = true;
-								break;
+#pragma unroll
+					for (int c = 0; c < NP; ++c) {
+						if (j < nwin && !bad) {
+							std::uint32_t spins = 0;
+							while (!agg_valid(lbv[i][c], epoch)) {
+								if (++spins > kSpinLimit) {
+									record_error(res, kDevErrTimeout);
+									bad = true;
+									break;
+								}
+								if ((spins & 63u) == 0 && aborted(res)) {
+									bad = true;
+									break;
+								}
+								__nanosleep(20);
+								lbv[i][c] = ld_relaxed64(&d_agg[c * static_cast<std::uint64_t>(ntiles) + t - 1 - j]);
 							}
-							if ((spins & 63u) == 0 && aborted(res)) {
-								bad = true;
-								break;
-							}
-							__nanosleep(20);
-							lbv[i] = ld128_relaxed(src);
 						}
 					}
 				}
 				if (__any_sync(kFull, bad)) {
 					failed = true;
 				} else {
-					std::uint32_t s_incl = 0, c_incl[3] = {0, 0, 0};
-#pragma unroll
-					for (int i = 0; i < kLB; ++i)
-						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 == W) {
-							s_incl	  = lbv[i].w & 3u;
-							c_incl[0] = lbv[i].x;
-							c_incl[1] = lbv[i].y;
-							c_incl[2] = lbv[i].z;
-						}
-					const int src_lane = static_cast<int>((W - 1) / kLB);
-					s_incl			   = __shfl_sync(kFull, s_incl, src_lane);
-					c_incl[0]		   = __shfl_sync(kFull, c_incl[0], src_lane);
-					c_incl[1]		   = __shfl_sync(kFull, c_incl[1], src_lane);
-					c_incl[2]		   = __shfl_sync(kFull, c_incl[2], src_lane);
-					std::uint32_t E	   = kIdent;
+					// this lane's words composed, farthest (earliest) tile first
+					WinElem r;
 #pragma unroll
 					for (int i = kLB - 1; i >= 0; --i)
-						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W)
-							E = compose_fast(E, lbv[i].w & 0xFu);
-					std::uint32_t x = E;
+						if (static_cast<std::uint32_t>(lane) * kLB + i < nwin)
+							r = r.then(WinElem::of<PATH, BR>(lbv[i]));
+					// suffix scan over the lanes: lane 0 ends with the whole window
 #pragma unroll
 					for (int off = 1; off < 32; off <<= 1) {
-						const std::uint32_t o = __shfl_down_sync(kFull, x, off);
+						const WinElem o = r.shfl_down<BR>(off);
 						if (lane + off < 32)
-							x = compose_fast(o, x);
+							r = o.then(r);
 					}
-					std::uint32_t ex = __shfl_down_sync(kFull, x, 1);
-					if (lane == 31)
-						ex = kIdent;
-					std::uint32_t st = PATH == kPathNone ? 0u : apply_fast(ex, s_incl);
-					std::uint32_t cs = 0, co = 0, cc = 0;
-#pragma unroll
-					for (int i = kLB - 1; i >= 0; --i)
-						if (static_cast<std::uint32_t>(lane) * kLB + i + 1 < W) {
-							std::uint32_t a0, a1, a2;
-							agg_counts<PATH>(lbv[i], st, a0, a1, a2);
-							cs += a0;
-							co += a1;
-							cc += a2;
-							if (PATH != kPathNone)
-								st = apply_fast(lbv[i].w & 0xFu, st);
-						}
-#pragma unroll
-					for (int off = 16; off > 0; off >>= 1) {
-						cs += __shfl_xor_sync(kFull, cs, off);
-						if (BR) {
-							co += __shfl_xor_sync(kFull, co, off);
-							cc += __shfl_xor_sync(kFull, cc, off);
-						}
-					}
-					s_t		= __shfl_sync(kFull, st, 0);
-					base[0] = c_incl[0] + cs;
-					base[1] = c_incl[1] + co;
-					base[2] = c_incl[2] + cc;
-					if (lane == 0) {
-						std::uint32_t c0, c1, c2;
-						agg_counts<PATH>(agg, s_t, c0, c1, c2);
-						const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, s_t);
-						st128_relaxed(&d_incl[t], make_uint4(base[0] + c0, base[1] + c1, base[2] + c2,
-															 kDIncl | (epoch << 8) | after));
-					}
+					r = r.shfl0<BR>();
+					const std::uint32_t p_prev = (s_prev >> 1) & 1u;
+					s_t		= PATH == kPathNone ? 0u : (s_prev ^ (r.q << 1));
+					base[0] = base_prev[0] + (p_prev ? r.c[1] : r.c[0]);
+					base[1] = base_prev[1] + (p_prev ? r.c[3] : r.c[2]);
+					base[2] = base_prev[2] + (p_prev ? r.c[5] : r.c[4]);
+					std::uint32_t c0, c1, c2;
+					agg_counts<PATH>(agg, s_t, c0, c1, c2);
+					s_prev		 = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, s_t);
+					base_prev[0] = base[0] + c0;
+					base_prev[1] = base[1] + c1;
+					base_prev[2] = base[2] + c2;
 				}
 			}
 			if (lane == 0) {
@@ -378,11 +421,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				sc.base[buf][1] = base[1];
 				sc.base[buf][2] = base[2];
 				if (!failed && t == ntiles - 1) {
-					std::uint32_t c0, c1, c2;
-					agg_counts<PATH>(agg, s_t, c0, c1, c2);
-					const unsigned long long ns = static_cast<unsigned long long>(base[0]) + c0;
-					const unsigned long long no = static_cast<unsigned long long>(base[1]) + c1;
-					const unsigned long long nc = static_cast<unsigned long long>(base[2]) + c2;
+					const unsigned long long ns = base_prev[0], no = base_prev[1], nc = base_prev[2];
 					res->n_struct	= ns;
 					res->n_open		= no;
 					res->n_close	= nc;
@@ -461,6 +500,31 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			if (hi < lo)
 				hi = lo;
 			return bit_range(lo, hi);
+		};
+
+		// The thread whose word holds the document's last byte records the end state
+		// (bracket-less kernels keep no toggle planes in their fronts, so the word's
+		// toggles are recomputed from the input; this runs once per scan).
+		auto end_of_document = [&](unsigned long long qw, std::uint32_t p_w) {
+			std::uint32_t endstate = 0, last_flag = 0, unclosed = 0;
+			if (PATH != kPathNone) {
+				const int lo = qw < a.o ? static_cast<int>(a.o - qw) : 0;
+				const int hi = static_cast<int>(doc_end - qw);
+				std::uint32_t D = 0;
+				for (int j = lo; j < hi; ++j)
+					D |= ((P->cls[a.base[qw + j]] & kClsDelim) ? 1u : 0u) << j;
+				const std::uint32_t elem = 1u | ((__popc(D) & 1u) << 2);
+				endstate				 = apply_fast(elem, p_w << 1);
+				last_flag				 = (D >> (hi - 1)) & 1u;
+				unclosed				 = ((endstate >> 1) & 1u) | last_flag;
+			}
+			res->unclosed = unclosed;
+			if (a.carry_out) {
+				a.carry_out->fstate		 = endstate;
+				a.carry_out->last_delim	 = last_flag;
+				a.carry_out->last_toggle = last_flag;
+				a.carry_out->unclosed	 = unclosed;
+			}
 		};
 
 		auto phase_a = [&](std::uint32_t k, WsFront& F) -> bool {
@@ -570,7 +634,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				for (int h = 0; h < 2; ++h) {
 					const std::uint32_t m0 = ex0[h] | F.dd[h], m1 = ~ex0[h] | F.dd[h];
 					std::uint32_t*		e  = h == 0 ? w0 : v;
-					e[0] = __popc(F.S[h] & ~m0) | (__popc(F.S[h] & ~m1) << 16);
+					F.sel0[h]			   = F.S[h] & ~m0;
+					F.sel1[h]			   = F.S[h] & ~m1;
+					e[0] = __popc(F.sel0[h]) | (__popc(F.sel1[h]) << 16);
 					if (BR) {
 						e[2] = __popc(F.O[h] & ~m0) | (__popc(F.O[h] & ~m1) << 16);
 						e[3] = __popc(F.C[h] & ~m0) | (__popc(F.C[h] & ~m1) << 16);
@@ -578,6 +644,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				}
 				OpParity()(w0, v);	// thread element = word 0 then word 1
 			} else {
+				F.sel0[0] = F.sel1[0] = F.S[0];
+				F.sel0[1] = F.sel1[1] = F.S[1];
 				OpSum3()(w0, v);
 			}
 			if (!BR)
@@ -591,6 +659,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				const std::uint32_t e = i < NL ? __shfl_up_sync(kFull, v[i], 1) : 0u;
 				F.ex[i]				  = lane == 0 ? 0u : e;
 			}
+			if (!BR && PATH != kPathNone)
+				F.ex[1] |= (w0[1] & 1u) << 1;
 			if (lane == 31)
 #pragma unroll
 				for (int i = 0; i < NL; ++i) sc.wtot[buf][warp][i] = v[i];
@@ -643,6 +713,44 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			}
 			const bool interior = static_cast<unsigned long long>(t) * kWsTile >= a.o
 							   && static_cast<unsigned long long>(t + 1) * kWsTile <= doc_end;
+			if constexpr (!BR) {
+				// bracket-less: pick each word's selection by its entry parity
+				std::uint32_t si = base[0] + off[0];
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					const unsigned long long qw = q0 + 32u * h;
+					std::uint32_t			 m	= p_w ? F.sel1[h] : F.sel0[h];
+					if (doc_end <= qw + 32 && doc_end > qw && valid_mask(qw, interior) != 0)
+						end_of_document(qw, p_w);
+					if (PATH != kPathNone && h == 0)
+						p_w ^= (p0[1] >> 1) & 1u;  // word 1 starts after word 0's toggles
+					const std::uint32_t	 pos0 = byte_base + static_cast<std::uint32_t>(qw - a.o);
+					const unsigned char* gb	  = a.base + qw;  // input bytes (global, L2-resident)
+					if (si + static_cast<std::uint32_t>(__popc(m)) <= cap_s && !want_chars && !want_pairs) {
+						std::uint32_t* out = a.pos + si;
+						si += __popc(m);
+						while (m) {
+							const int j = __ffs(m) - 1;
+							m &= m - 1;
+							*out++ = pos0 + j;
+						}
+					} else {
+						while (m) {
+							const int j = __ffs(m) - 1;
+							m &= m - 1;
+							if (si < cap_s) {
+								a.pos[si] = pos0 + j;
+								if (want_chars)
+									a.chars[si] = gb[j];
+								if (want_pairs)
+									a.pair[si] = -1;
+							}
+							++si;
+						}
+					}
+				}
+				return true;
+			} else {
 #pragma unroll
 			for (int h = 0; h < 2; ++h) {
 				const unsigned long long qw = q0 + 32u * h;
@@ -749,6 +857,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 					a.mask[(byte_base + static_cast<std::uint32_t>(qw - a.o)) >> 5] = mask;
 			}
 			return true;
+			}
 		};
 
 		// A runs kAhead tiles ahead of B.  The fronts rotate by register moves, which

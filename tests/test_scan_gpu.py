@@ -100,6 +100,36 @@ def test_random_alphabet_vs_oracle(scanners, grammar, n):
     compare(run(scanners[grammar], data), e, f"{grammar}/{n}")
 
 
+@pytest.mark.parametrize("grammar", GRAMMARS)
+@pytest.mark.parametrize("outputs", ["offsets", "chars", "pairs", "chars+pairs"])
+def test_output_subsets(scanners, grammar, outputs):
+    """Structural offsets with each subset of the optional outputs and no mask
+    bitmap: the bracket-less kernels choose their output route by these flags."""
+    from tests_alphabets import ALPHABETS
+    plan = plan_bytes(grammar)
+    want_chars, want_pairs = "chars" in outputs, "pairs" in outputs
+    cases = [(synth.alpha(41, ALPHABETS[grammar], 33), 0),
+             (synth.alpha(43, ALPHABETS[grammar], (1 << 20) + 5), 0),
+             (synth.alpha(47, ALPHABETS[grammar], (1 << 20) + 5), 7)]
+    if grammar == "csv":
+        cases.append((synth.csv_doc(5, 3 << 20), 0))
+    for data, off in cases:
+        e = expected_from_oracle(plan, data)
+        buf, ptr = to_dev(data, off)
+        r = scanners[grammar].scan_device(ptr, data.size, want_pairs=want_pairs, want_chars=want_chars)
+        torch.cuda.synchronize()
+        g = r.to_numpy()
+        name = f"{grammar}/{outputs}/{data.size}/off{off}"
+        assert np.array_equal(g["pos"], e["pos"]), name
+        if want_chars:
+            assert np.array_equal(g["chars"], e["chars"]), name
+        if want_pairs:
+            assert np.array_equal(g["pair"], e["pair"]), name
+        meta = (r.unclosed_mode, r.balanced, r.well_formed, r.max_depth)
+        assert tuple(meta) == tuple(e["meta"]), f"{name}: flags {meta} != {e['meta']}"
+        del buf
+
+
 @pytest.mark.parametrize("offset", [1, 3, 8, 15])
 def test_unaligned_input(scanners, offset):
     for g in ("json", "csv", "toml"):
