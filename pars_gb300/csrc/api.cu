@@ -433,7 +433,8 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	const bool	   fast	 = s.path != kPathGeneric;
 	const uint64_t tile	 = (fast && use_ws(s.path)) ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;
 	const uint64_t ntiles = (total + tile - 1) / tile;
-	const size_t tdesc = fast ? 2 * sizeof(uint4) : sizeof(TileDescG);  // fast: AGG + INCL words
+	// fast kernels: AGG and INCL words, three 64-bit planes each
+	const size_t tdesc = fast ? 6 * sizeof(uint64_t) : sizeof(TileDescG);
 	if (int r = grow(ctx, ctx->tiles, ntiles * tdesc))
 		return r;
 	// The bracket-less warp-specialised kernels keep no per-byte toggle planes, so a

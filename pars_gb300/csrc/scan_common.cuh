@@ -116,37 +116,6 @@ __device__ __forceinline__ T warp_max(T v) {
 	return v;
 }
 
-// 128-bit single-copy-atomic descriptor access.
-__device__ __forceinline__ uint4 ld128_relaxed(const uint4* p) {
-	std::uint64_t lo, hi;
-	asm volatile(
-		"{ .reg .b128 t; ld.relaxed.gpu.global.b128 t, [%2]; mov.b128 {%0, %1}, t; }"
-		: "=l"(lo), "=l"(hi)
-		: "l"(p)
-		: "memory");
-	return make_uint4(static_cast<std::uint32_t>(lo), static_cast<std::uint32_t>(lo >> 32),
-					  static_cast<std::uint32_t>(hi), static_cast<std::uint32_t>(hi >> 32));
-}
-
-__device__ __forceinline__ void st128_release(uint4* p, uint4 v) {
-	const std::uint64_t lo = v.x | (static_cast<std::uint64_t>(v.y) << 32);
-	const std::uint64_t hi = v.z | (static_cast<std::uint64_t>(v.w) << 32);
-	asm volatile("{ .reg .b128 t; mov.b128 t, {%1, %2}; st.release.gpu.global.b128 [%0], t; }" ::"l"(p),
-				 "l"(lo), "l"(hi)
-				 : "memory");
-}
-
-// Relaxed 128-bit store: a look-back word is self-contained (flag, epoch and
-// payload travel together), so readers need no ordering beyond single-copy
-// atomicity, and the writer need not wait for its earlier output stores.
-__device__ __forceinline__ void st128_relaxed(uint4* p, uint4 v) {
-	const std::uint64_t lo = v.x | (static_cast<std::uint64_t>(v.y) << 32);
-	const std::uint64_t hi = v.z | (static_cast<std::uint64_t>(v.w) << 32);
-	asm volatile("{ .reg .b128 t; mov.b128 t, {%1, %2}; st.relaxed.gpu.global.b128 [%0], t; }" ::"l"(p),
-				 "l"(lo), "l"(hi)
-				 : "memory");
-}
-
 __device__ __forceinline__ void fence_acq_rel() {
 	asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }

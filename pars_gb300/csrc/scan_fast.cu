@@ -186,8 +186,9 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 	const int			tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const DevPlan*		P	= a.plan;
 	DevResult*			res = a.res;
-	uint4*				d_agg  = static_cast<uint4*>(a.tiles);
-	uint4*				d_incl = d_agg + a.ntiles;
+	std::uint64_t*		d_agg  = static_cast<std::uint64_t*>(a.tiles);	// AGG words, planes [3][ntiles]
+	std::uint64_t*		d_incl = d_agg + 3 * a.ntiles;					// INCL words, planes [3][ntiles]
+	const std::uint64_t nt	   = a.ntiles;
 	const std::uint32_t G	   = gridDim.x;
 	const std::uint32_t epoch  = a.epoch & 0x3FFFFFu;
 	const std::uint32_t ntiles = static_cast<std::uint32_t>(a.ntiles);
@@ -467,11 +468,11 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 				std::uint32_t cs, co, cc;
 				agg_counts<PATH>(d, init_state, cs, co, cc);
 				const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(tot[3], init_state);
-				st128_relaxed(&d_incl[0], make_uint4(base0[0] + cs, base0[1] + co, base0[2] + cc,
-													 kDIncl | (epoch << 8) | after));
+				st_desc(d_incl, nt, 0, make_uint4(base0[0] + cs, base0[1] + co, base0[2] + cc,
+												  kDIncl | (epoch << 8) | after));
 			} else {
 				d.w |= kDAgg | (epoch << 8);
-				st128_relaxed(&d_agg[t], d);
+				st_desc(d_agg, nt, t, d);
 			}
 		}
 	};
@@ -488,9 +489,9 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 			const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
 			lbv[i]				  = make_uint4(0, 0, 0, 0);
 			if (j + 1 < W)
-				lbv[i] = ld128_relaxed(&d_agg[t - 1 - j]);
+				lbv[i] = ld_desc(d_agg, nt, t - 1 - j);
 			else if (j + 1 == W)
-				lbv[i] = ld128_relaxed(&d_incl[t - W]);
+				lbv[i] = ld_desc(d_incl, nt, t - W);
 		}
 	};
 	auto fold = [&](std::uint32_t t, uint4 (&lbv)[kLB]) {
@@ -502,7 +503,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 				const std::uint32_t j = static_cast<std::uint32_t>(lane) * kLB + i;
 				if (j < W) {
 					const bool			incl_slot = (j + 1 == W);
-					const uint4*		src		  = incl_slot ? &d_incl[t - W] : &d_agg[t - 1 - j];
+					const std::uint64_t* src	  = incl_slot ? d_incl : d_agg;
+					const std::uint64_t	 idx	  = incl_slot ? t - W : t - 1 - j;
 					const std::uint32_t want	  = incl_slot ? 2u : 1u;
 					std::uint32_t		spins	  = 0;
 					while (!((lbv[i].w >> 30) == want && ((lbv[i].w >> 8) & 0x3FFFFFu) == epoch)) {
@@ -516,7 +518,7 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 							break;
 						}
 						__nanosleep(32);
-						lbv[i] = ld128_relaxed(src);
+						lbv[i] = ld_desc(src, nt, idx);
 					}
 				}
 			}
@@ -601,8 +603,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) k_scan_fast(const ScanArgs a)
 			std::uint32_t cs, co, cc;
 			agg_counts<PATH>(sc.agg[buf], s_t, cs, co, cc);
 			const std::uint32_t after = PATH == kPathNone ? 0u : apply_fast(sc.tile_elem[buf], s_t);
-			st128_relaxed(&d_incl[t], make_uint4(base[0] + cs, base[1] + co, base[2] + cc,
-												 kDIncl | (epoch << 8) | after));
+			st_desc(d_incl, nt, t, make_uint4(base[0] + cs, base[1] + co, base[2] + cc,
+											  kDIncl | (epoch << 8) | after));
 		}
 		const std::uint32_t vm	 = F.vm;
 		const std::uint32_t e_t	 = s_t & 1u, p_t = (s_t >> 1) & 1u;
