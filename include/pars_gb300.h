@@ -161,6 +161,35 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
                       uint32_t flags, void* stream, pars_device_result* out);
 
+/* ---- scan without allocation ---------------------------------------------- */
+/* No counterpart in the reference (whose scanner always owns a DeviceCache that
+ * grows with cudaMalloc, pipeline.cuh:562-714).  For callers that must not allocate
+ * device memory on their scan path: stage 1 (R1-R5) of one document, structural
+ * offsets only, into caller-owned device memory.  The call allocates nothing: its
+ * scratch is one fixed device array of about 1 MiB compiled into the library, which
+ * bounds the input to PARS_NOALLOC_MAX_BYTES (larger inputs: PARS_ERANGE).
+ *   - d_struct receives the first min(n_struct, cap) offsets; d_result (device
+ *     memory) receives n_struct (n_struct > cap means the offsets were cut off),
+ *     unclosed_mode and a status (0, or PARS_ETIMEDOUT if a device wait gave up).
+ *   - Brackets, pairs, chars and masks are not produced; plans with an escape
+ *     automaton run the general descriptor kernel.
+ *   - The call does not synchronise; results are ready when `stream` reaches them.
+ *   - All calls on a device share the one scratch array, whatever their context or
+ *     stream: calls that overlap in time race.  Serialise them.
+ *   - The first call on a device looks up the scratch's address: make it before
+ *     any stream capture. */
+#define PARS_NOALLOC_MAX_BYTES 134217728ull      /* 128 MiB */
+
+typedef struct pars_noalloc_result {
+  uint64_t n_struct;
+  int32_t unclosed_mode;
+  int32_t status;
+} pars_noalloc_result;
+
+int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_t* d_in, uint64_t n,
+                             uint32_t* d_struct, uint64_t cap, pars_noalloc_result* d_result,
+                             void* stream);
+
 /* ---- profiling ------------------------------------------------------------ */
 /* cf. stage_times (pipeline.cuh:746-748, 767-774, 998-1011): when enabled, the
  * context brackets its own launches with CUDA events on the caller's stream;

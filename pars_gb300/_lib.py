@@ -57,6 +57,15 @@ class ChunkCarry(ctypes.Structure):
                 ("bracket_base", ctypes.c_uint64), ("byte_base", ctypes.c_uint64)]
 
 
+class NoAllocResult(ctypes.Structure):
+    """pars_noalloc_result (lives in device memory; read it back to inspect)."""
+    _fields_ = [("n_struct", ctypes.c_uint64), ("unclosed_mode", ctypes.c_int32),
+                ("status", ctypes.c_int32)]
+
+
+PARS_NOALLOC_MAX_BYTES = 134217728
+
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "pars_version": (ctypes.c_int, []),
@@ -84,6 +93,9 @@ SIGNATURES = {
     "pars_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                         ctypes.POINTER(ctypes.c_float)]),
     "pars_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "pars_scan_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 _LIB = None

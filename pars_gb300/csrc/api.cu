@@ -1076,3 +1076,87 @@ uint64_t pars_launch_count(const pars_ctx* ctx) {
 }
 
 }  // extern "C"
+
+// ================================================================================
+// Scan without allocation
+// ================================================================================
+namespace pars {
+cudaError_t noalloc_scratch(int device, unsigned char** addr);
+const void* noalloc_finish_kernel();
+}  // namespace pars
+
+extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_t* d_in, uint64_t n,
+										uint32_t* d_struct, uint64_t cap, pars_noalloc_result* d_result,
+										void* stream) {
+	static_assert(sizeof(TileDescG) <= 128, "descriptor scratch is sized for 128-byte descriptors");
+	static_assert(6 * sizeof(uint64_t) <= 128 * 2, "fast descriptors fit the descriptor scratch");
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !d_result || (n && !d_in) || (cap && !d_struct))
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	if (n > PARS_NOALLOC_MAX_BYTES)
+		return fail(ctx, PARS_ERANGE, "input larger than the fixed scratch allows (128 MiB)");
+	cudaSetDevice(ctx->device);
+	unsigned char* scr = nullptr;
+	CK(noalloc_scratch(ctx->device, &scr));
+	cudaStream_t st	 = static_cast<cudaStream_t>(stream);
+	ResBlock*	 rb	 = reinterpret_cast<ResBlock*>(scr);
+	Counters*	 ctr = reinterpret_cast<Counters*>(scr + kNoAllocRbBytes);
+	void*		 tiles = scr + kNoAllocRbBytes + kNoAllocCtrBytes;
+
+	const uint64_t o	  = reinterpret_cast<uintptr_t>(d_in) & 15u;
+	const uint8_t* base	  = d_in - o;
+	const uint64_t total  = o + n;
+	const bool	   ws	  = use_ws(pl->path);
+	const int	   path	  = ws ? pl->path : kPathGeneric;
+	const bool	   br	  = pl->host.has_brackets != 0;
+	const uint64_t tile	  = ws ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;
+	const uint64_t ntiles = (total + tile - 1) / tile;
+	const uint64_t desc	  = ntiles * (ws ? 3 * sizeof(uint64_t) : sizeof(TileDescG));
+	// what must start at zero: the result block, the counters, the descriptors in use
+	CK(cudaMemsetAsync(scr, 0, kNoAllocRbBytes + kNoAllocCtrBytes + desc, st));
+	if (n) {
+		if (ws) {
+			if (int r = ensure_fast_config(ctx, path, br))
+				return r;
+		} else if (int r = ensure_scan_config(ctx, path)) {
+			return r;
+		}
+		ScanArgs a {};
+		a.base	   = base;
+		a.o		   = o;
+		a.n		   = n;
+		a.ntiles   = ntiles;
+		a.copy_end = (total + 15) & ~uint64_t(15);
+		a.plan	   = pl->dev;
+		a.pos	   = d_struct;
+		a.cap_s	   = cap;
+		a.cap_b	   = 0;
+		a.tiles	   = tiles;
+		a.ctr	   = ctr;
+		a.res	   = &rb->r;
+		a.key_hist = rb->key_hist;
+		a.epoch	   = next_epoch(ctx);
+		a.flags	   = 0;
+		if (ws) {
+			const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[path * 2 + (br ? 1 : 0)]));
+			WsArgs		wa {a, total / 128};
+			CUtensorMap map;
+			if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+				return r;
+			void* wargs[] = {&wa, &map};
+			CK(cudaLaunchCooperativeKernel(fast_kernel(path, br), dim3(grid), dim3(fast_threads(path)), wargs,
+										   fast_smem(path), st));
+		} else {
+			const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[path]));
+			void*	  args[] = {&a};
+			CK(cudaLaunchCooperativeKernel(scan_kernel(path), dim3(grid), dim3(kScanThreads), args,
+										   scan_smem_bytes(path), st));
+		}
+		ctx->launches++;
+	}
+	DevResult* r		= &rb->r;
+	void*	   fargs[] = {&r, &d_result};
+	CK(cudaLaunchKernel(noalloc_finish_kernel(), dim3(1), dim3(1), fargs, 0, st));
+	ctx->launches++;
+	return 0;
+}

@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include "pars_gb300.h"
+
 namespace pars {
 
 // Scan-kernel paths.  A plan maps to one of them when it is loaded:
@@ -100,6 +102,15 @@ struct ResBlock {
 	DevResult	 r;
 	unsigned int key_hist[2048];
 };
+
+// Fixed scratch of pars_scan_device_noalloc: [result block][counters][tile
+// descriptors], each part on a 256-byte boundary.  Sized for the largest input it
+// accepts with the largest descriptor (the general kernel's, one per 16 KiB tile).
+constexpr unsigned long long kNoAllocRbBytes	= (sizeof(ResBlock) + 255) & ~255ull;
+constexpr unsigned long long kNoAllocCtrBytes	= 256;
+constexpr unsigned long long kNoAllocMaxTiles	= (PARS_NOALLOC_MAX_BYTES + 16 + 16383) / 16384;
+constexpr unsigned long long kNoAllocDescBytes	= 128 * kNoAllocMaxTiles;
+constexpr unsigned long long kNoAllocScratchBytes = kNoAllocRbBytes + kNoAllocCtrBytes + kNoAllocDescBytes;
 
 // State at a chunk boundary (device resident; chained chunk to chunk).
 struct DevCarry {

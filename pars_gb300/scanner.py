@@ -182,6 +182,16 @@ class Scanner:
               self.ctx.handle)
         return DeviceResult(r, n)
 
+    def scan_device_noalloc(self, d_ptr: int, n: int, d_struct: int, cap: int, d_result: int,
+                            stream: int = 0) -> None:
+        """pars_scan_device_noalloc: structural offsets into caller-owned device memory
+        (`d_struct`, room for `cap` offsets) and a pars_noalloc_result at `d_result`
+        (device memory).  Allocates nothing; does not synchronise."""
+        check(lib().pars_scan_device_noalloc(self.ctx.handle, self.plan_id, ctypes.c_void_p(d_ptr), n,
+                                             ctypes.c_void_p(d_struct), cap, ctypes.c_void_p(d_result),
+                                             ctypes.c_void_p(stream)),
+              self.ctx.handle)
+
     def scan_tensor(self, t, **kw) -> DeviceResult:
         """scan_device on a contiguous uint8 CUDA tensor."""
         import torch

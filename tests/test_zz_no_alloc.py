@@ -1,0 +1,88 @@
+"""pars_scan_device_noalloc (fixed device scratch, caller-owned outputs) against
+pars_scan_device on the same inputs: two different documents scanned back to back
+through the no-allocation entry point must each match the allocating one."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import plan_bytes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from pars_gb300 import Context, Scanner, synth  # noqa: E402
+from pars_gb300._lib import PARS_NOALLOC_MAX_BYTES, NoAllocResult, ParsError  # noqa: E402
+
+
+def docs(grammar):
+    if grammar == "json":
+        return [synth.json_doc(3, 3 << 20), synth.json_doc(4, (5 << 20) + 11)]
+    return [synth.csv_doc(3, 3 << 20), synth.csv_doc(4, (5 << 20) + 11)]
+
+
+def read_result(t):
+    raw = t.cpu().numpy().tobytes()
+    return NoAllocResult.from_buffer_copy(raw)
+
+
+@pytest.mark.parametrize("grammar", ["csv", "json", "toml", "clike"])
+def test_noalloc_matches_scan_device(grammar):
+    ctx = Context(0)
+    sc = Scanner(plan_bytes(grammar), ctx=ctx)
+    inputs = [torch.from_numpy(d).cuda() for d in docs(grammar)]
+    cap = max(int(t.numel()) for t in inputs)
+    outs = [torch.zeros(cap, dtype=torch.int32, device="cuda") for _ in inputs]
+    results = [torch.zeros(ctypes.sizeof(NoAllocResult), dtype=torch.uint8, device="cuda") for _ in inputs]
+    stream = torch.cuda.current_stream().cuda_stream
+    # two calls in a row on one stream, then compare each with the allocating path
+    for t, o, r in zip(inputs, outs, results):
+        sc.scan_device_noalloc(t.data_ptr(), t.numel(), o.data_ptr(), cap, r.data_ptr(), stream)
+    torch.cuda.synchronize()
+    for i, (t, o, r) in enumerate(zip(inputs, outs, results)):
+        got = read_result(r)
+        ref = sc.scan_tensor(t)
+        torch.cuda.synchronize()
+        exp = ref.to_numpy()["pos"]
+        assert got.status == 0, f"{grammar}/{i}: status {got.status}"
+        assert got.n_struct == exp.size, f"{grammar}/{i}: n_struct {got.n_struct} != {exp.size}"
+        assert got.unclosed_mode == ref.unclosed_mode, f"{grammar}/{i}: unclosed_mode"
+        pos = o[:exp.size].cpu().numpy().view(np.uint32)
+        assert np.array_equal(pos, exp), f"{grammar}/{i}: offsets differ"
+    # once the library is loaded, a call leaves the device's free memory unchanged
+    free0 = torch.cuda.mem_get_info()[0]
+    sc.scan_device_noalloc(inputs[0].data_ptr(), inputs[0].numel(), outs[0].data_ptr(), cap,
+                           results[0].data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_truncates_at_cap_and_reports_full_count():
+    ctx = Context(0)
+    sc = Scanner(plan_bytes("csv"), ctx=ctx)
+    t = torch.from_numpy(synth.csv_doc(9, 1 << 20)).cuda()
+    exp = sc.scan_tensor(t).to_numpy()["pos"]
+    cap = exp.size // 3
+    o = torch.full((cap + 64,), -1, dtype=torch.int32, device="cuda")
+    r = torch.zeros(ctypes.sizeof(NoAllocResult), dtype=torch.uint8, device="cuda")
+    sc.scan_device_noalloc(t.data_ptr(), t.numel(), o.data_ptr(), cap, r.data_ptr(),
+                           torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = read_result(r)
+    assert got.n_struct == exp.size
+    a = o.cpu().numpy()
+    assert np.array_equal(a[:cap].view(np.uint32), exp[:cap])
+    assert np.all(a[cap:] == -1)
+
+
+def test_noalloc_empty_and_too_large():
+    ctx = Context(0)
+    sc = Scanner(plan_bytes("csv"), ctx=ctx)
+    r = torch.full((ctypes.sizeof(NoAllocResult),), 0xAB, dtype=torch.uint8, device="cuda")
+    sc.scan_device_noalloc(0, 0, 0, 0, r.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = read_result(r)
+    assert (got.n_struct, got.unclosed_mode, got.status) == (0, 0, 0)
+    t = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(ParsError):
+        sc.scan_device_noalloc(t.data_ptr(), PARS_NOALLOC_MAX_BYTES + 1, 0, 0, r.data_ptr(), 0)
