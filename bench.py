@@ -71,62 +71,73 @@ def traffic_from_profiles(kernel: str):
 
 
 class Clocks:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """Samples the SM clock and the clock-event (throttle) reasons of one GPU during the
+    timed region, every millisecond, straight from NVML (the driver's libnvidia-ml;
+    read-only queries).  Falls back to no samples when NVML is unavailable."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, index: int):
-        self.index = index
-        self.proc = None
-        self.lines: list[str] = []
+    def __init__(self, cuda_index: int):
+        self.cuda_index = cuda_index
+        self.samples: list[tuple[int, int]] = []
+        self.max_mhz = None
+        self.stop = threading.Event()
         self.t = None
+        self.nvml = None
+        self.handle = None
+
+    def _open(self):
+        import ctypes
+        import torch
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return False
+        p = torch.cuda.get_device_properties(self.cuda_index)
+        bus = f"{p.pci_domain_id:08x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0".encode()
+        h = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(h)) != 0:
+            return False
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = int(mx.value)
+        self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.nvml, self.handle = nv, h
+        return True
+
+    def _run(self):
+        import ctypes
+        mhz, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.handle, ctypes.byref(rs)) == 0:
+                self.samples.append((int(mhz.value), int(rs.value)))
+            time.sleep(0.001)
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            if self._open():
+                self.t = threading.Thread(target=self._run, daemon=True)
+                self.t.start()
         except Exception:
-            self.proc = None
+            self.t = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
     def __exit__(self, *exc):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except Exception:
-                self.proc.kill()
-            if self.t:
-                self.t.join(timeout=2)
+        self.stop.set()
+        if self.t:
+            self.t.join(timeout=2)
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"]}
+        reasons = set()
+        for _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(m for m, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml"}
 
 
 def plan(name: str) -> bytes:
@@ -334,8 +345,8 @@ def main():
                        "n_struct": r.n_struct, "kernel_path": r.kernel_path},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": traffic_from_profiles("k_scan"),
-                         "peak_kind": peak_kind, "kernel": "k_scan<doubled>",
+                         "traffic": traffic_from_profiles("k_scan_ws"),
+                         "peak_kind": peak_kind, "kernel": "k_scan_ws<doubled>",
                          "kernel_ms": round(scan_ms, 4), "algorithmic_bytes": int(alg_bytes)},
             "e2e": e2e,
             "gpu_launches": int(launches),

@@ -1,0 +1,33 @@
+"""Run the scan a few times on one seeded synthetic document, for profilers.
+
+    python -m pars_gb300.profile_run <csv|json> <MiB> [repeats] [--pairs]
+
+Loads the plan from tests/golden/plans, generates the document with the library's
+seeded generators, scans it `repeats` times on the current CUDA device and prints
+the structural count.  Profilers select the launch they want (e.g. ncu -k/-s/-c).
+"""
+import os
+import sys
+
+
+def main(argv):
+    import torch
+    from pars_gb300 import Scanner, synth
+    grammar, mib = argv[0], int(argv[1])
+    repeats = int(argv[2]) if len(argv) > 2 and not argv[2].startswith("-") else 3
+    pairs = "--pairs" in argv
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "tests", "golden", "plans", f"{grammar}.plan"), "rb") as f:
+        plan = f.read()
+    data = synth.csv_doc(7, mib << 20) if grammar == "csv" else synth.json_doc(7, mib << 20)
+    t = torch.from_numpy(data).cuda()
+    sc = Scanner(plan)
+    r = None
+    for _ in range(repeats):
+        r = sc.scan_tensor(t, want_pairs=pairs)
+    torch.cuda.synchronize()
+    print(grammar, data.size, r.n_struct, r.n_brackets, r.kernel_path)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
