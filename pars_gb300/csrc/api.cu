@@ -41,6 +41,7 @@ int		   scan_ws_smem_bytes();
 const void* scan_ws_kernel(int path, bool brackets);
 const void* scan_fast_kernel(int path, bool brackets);
 int		   sort_tile_keys();
+const void* bchar_gather_kernel();
 struct SortPass;
 __global__ void k_sort_pass(const SortPass p);
 __global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, unsigned int shift,
@@ -123,6 +124,8 @@ struct pars_ctx {
 	cudaEvent_t prof[3] = {nullptr, nullptr, nullptr};
 	bool		prof_pairs = false;
 	uint64_t	launches   = 0;
+	// the document of the current whole-document scan (R6 gathers bracket bytes)
+	const uint8_t* cur_in = nullptr;
 };
 
 namespace {
@@ -298,7 +301,10 @@ int analyse_plan(const pars_scan_plan& p, DevPlan& h) {
 	} else if (p.n_descs == 1) {
 		const pars_lex_desc& D = p.descs[0];
 		const int dl = D.delim, es = D.escape;
-		if (dl != 0 && es != 0 && es != dl && isomorphic(D, kEscape, dl, es))
+		// the escape path counts the first byte after a backslash run by its classes,
+		// so the backslash itself must be neither punctuation nor a bracket
+		if (dl != 0 && es != 0 && es != dl && isomorphic(D, kEscape, dl, es)
+			&& !(h.cls[es] & (kClsStruct | kClsOpen | kClsClose)))
 			path = kPathEscape;
 		else if (dl != 0 && isomorphic(D, kDoubled, dl, -1))
 			path = kPathDoubled;
@@ -348,10 +354,10 @@ struct Scan {
 	DevCarry*	   carry_out;
 };
 
-// The parity / doubled / no-descriptor paths run the warp-specialised kernel
-// (scan_ws.cu); the escape path runs scan_fast.cu; everything else scan.cu.
+// The no-descriptor, parity, doubled and escape paths run the warp-specialised
+// kernel (scan_ws.cu); everything else runs the general kernel (scan.cu).
 bool use_ws(int path) {
-	return path == kPathNone || path == kPathParity || path == kPathDoubled;
+	return path == kPathNone || path == kPathParity || path == kPathDoubled || path == kPathEscape;
 }
 
 const void* fast_kernel(int path, bool br) {
@@ -504,6 +510,9 @@ PairArgs pair_args(pars_ctx* ctx, const Plan* pl, uint32_t flags, const uint32_t
 	PairArgs p {};
 	p.depth	   = static_cast<const int32_t*>(ctx->depth.p);
 	p.bchar	   = static_cast<const uint8_t*>(ctx->bchar.p);
+	p.in	   = ctx->cur_in;
+	p.bpos	   = static_cast<const uint32_t*>(ctx->bpos.p);
+	p.bchar_out = static_cast<uint8_t*>(ctx->bchar.p);
 	p.bsi	   = static_cast<const uint32_t*>(ctx->bsi.p);
 	p.order	   = const_cast<uint32_t*>(order);
 	p.pair	   = (flags & PARS_WANT_PAIRS) ? static_cast<int32_t*>(ctx->pair.p) : nullptr;
@@ -715,10 +724,17 @@ int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, u
 		if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
 			return r;
 		Scan s {d_in, n, flags, st, path, nullptr, nullptr};
+		ctx->cur_in = d_in;
 		if (ctx->profiling)
 			CK(cudaEventRecord(ctx->prof[0], st));
 		if (int r = launch_scan(ctx, pl, s))
 			return r;
+		if (!run_pairs && pl->host.has_brackets) {
+			// no R6: the bracket bytes come straight from the document
+			void* ga[] = {&ctx->bpos.p, &ctx->res, &ctx->cap_b, &d_in, &ctx->bchar.p};
+			CK(cudaLaunchKernel(bchar_gather_kernel(), dim3(ctx->num_sms * 4), dim3(256), ga, 0, st));
+			ctx->launches++;
+		}
 		if (ctx->profiling)
 			CK(cudaEventRecord(ctx->prof[1], st));
 		if (run_pairs)
@@ -991,7 +1007,7 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 	const int path = pl->path == kPathEscape ? kPathGeneric : pl->path;
 	DevCarry* cin  = ctx->carry + (ctx->chunk_index & 1);
 	DevCarry* cout = ctx->carry + ((ctx->chunk_index + 1) & 1);
-	Scan s {d_chunk, n, PARS_WANT_PAIRS | PARS_WANT_CHARS, st, path, cin, cout};
+	Scan s {d_chunk, n, PARS_WANT_PAIRS | PARS_WANT_CHARS | kScanOwnBchar, st, path, cin, cout};
 	if (int r = launch_scan(ctx, pl, s, ctx->chunk_index == 0))
 		return r;
 	ctx->chunk_index++;
@@ -1003,6 +1019,8 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry, uint32_t flags,
 					  void* stream, pars_device_result* out) {
 	Plan* pl = get_plan(ctx, plan_id);
+	if (ctx)
+		ctx->cur_in = nullptr;  // chunk inputs are gone: the scans wrote the bracket bytes
 	if (!pl || !carry || !out)
 		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
 	cudaSetDevice(ctx->device);
@@ -1106,7 +1124,9 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 	const uint64_t o	  = reinterpret_cast<uintptr_t>(d_in) & 15u;
 	const uint8_t* base	  = d_in - o;
 	const uint64_t total  = o + n;
-	const bool	   ws	  = use_ws(pl->path);
+	// the escape path may need a rerun on the general kernel, which needs the host:
+	// here escape plans run the general kernel directly
+	const bool	   ws	  = use_ws(pl->path) && pl->path != kPathEscape;
 	const int	   path	  = ws ? pl->path : kPathGeneric;
 	const bool	   br	  = pl->host.has_brackets != 0;
 	const uint64_t tile	  = ws ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;

@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort
 	for (unsigned long long r = blockIdx.x * 256ull + tid; r < npairs; r += gridDim.x * 256ull) {
 		const std::uint32_t ia = a.order[2 * r];
 		if (2 * r + 1 >= n) {  // odd count: the last entry has no partner
+			if (a.in)
+				a.bchar_out[ia] = a.in[a.bpos[ia]];
 			if (want) {
 				if (a.bpair)
 					a.bpair[ia] = -1;
@@ -264,7 +266,16 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort
 			continue;
 		}
 		const std::uint32_t ib = a.order[2 * r + 1];
-		const std::uint8_t	ca = a.bchar[ia], cb = a.bchar[ib];
+		std::uint8_t		ca, cb;
+		if (a.in) {
+			ca				= a.in[a.bpos[ia]];
+			cb				= a.in[a.bpos[ib]];
+			a.bchar_out[ia] = ca;
+			a.bchar_out[ib] = cb;
+		} else {
+			ca = a.bchar[ia];
+			cb = a.bchar[ib];
+		}
 		const bool ok = s_open[ca] && s_close[cb] && s_first[ca] == (0x100u | cb);
 		if (!ok)
 			bad = 1;
@@ -302,6 +313,18 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort
 			__threadfence();
 		}
 	}
+}
+
+// Bracket bytes gathered from the document when R6 does not run.
+__global__ void k_bchar_gather(const std::uint32_t* bpos, const DevResult* res, unsigned long long cap_b,
+							   const std::uint8_t* in, std::uint8_t* bchar) {
+	const unsigned long long n = res->n_brackets < cap_b ? res->n_brackets : cap_b;
+	for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += gridDim.x * 256ull)
+		bchar[i] = in[bpos[i]];
+}
+
+const void* bchar_gather_kernel() {
+	return reinterpret_cast<const void*>(&k_bchar_gather);
 }
 
 int sort_tile_keys() {

@@ -29,6 +29,12 @@ constexpr std::uint32_t kClsOpen   = 1u << 8;
 constexpr std::uint32_t kClsClose  = 1u << 16;
 constexpr std::uint32_t kClsDelim  = 1u << 24;
 
+// Internal scan flag (ScanArgs::flags, above the public PARS_* bits): the scan
+// kernel itself writes each bracket's byte.  Set for chunked scans, whose input is
+// gone by the time R6 runs; a whole-document scan leaves it to R6, which gathers
+// the bytes from the still-resident input.
+constexpr std::uint32_t kScanOwnBchar = 1u << 16;
+
 struct DevPlan {
 	std::uint32_t cls[256];			   // R1 classifier (classify.hpp:39-55) + fast-path delim
 	std::uint8_t  is_open[256];		   // nest.hpp:24-30
@@ -155,7 +161,10 @@ struct ScanArgs {
 
 struct PairArgs {
 	const std::int32_t*	 depth;		// [n_brackets] keys
-	const std::uint8_t*	 bchar;
+	const std::uint8_t*	 bchar;		// bracket bytes written by the scan (when `in` is null)
+	const std::uint8_t*	 in;		// the document: bracket bytes are gathered from it
+	const std::uint32_t* bpos;		// [n_brackets] byte offsets (with `in`)
+	std::uint8_t*		 bchar_out; // [n_brackets] gathered bracket bytes (with `in`)
 	const std::uint32_t* bsi;
 	std::uint32_t*		 order;		// [n_brackets] bracket indices sorted by (key, index)
 	std::int32_t*		 pair;		// structural space, may be null

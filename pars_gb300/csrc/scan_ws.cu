@@ -1,5 +1,6 @@
 // scan_ws.cu — warp-specialised fused R1..R5 scan for plans whose lexical layer is
-// empty, a quote-parity automaton or a doubled-delimiter automaton (the CSV shape).
+// empty, a quote-parity automaton, a doubled-delimiter automaton (the CSV shape) or
+// a quote automaton with a backslash escape (the JSON shape).
 //
 // Data movement.  The document is viewed as a 2-D tensor of 128-byte rows and
 // streamed in 32 KiB tiles (256 rows) by TMA tensor copies with the 128-byte
@@ -62,6 +63,7 @@ constexpr int kWsTile	 = kWorkers * 32 * 64;		  // 32 KiB: 512 threads x 64 byte
 constexpr int kWsRows	 = kWsTile / 128;			  // 256 rows of 128 bytes
 constexpr int kAhead	 = 3;						  // workers run phase A this many tiles ahead of B
 constexpr int kBufs		 = 4;						  // hand-off buffers (>= kAhead + 1)
+constexpr int kListCap	 = 512;						  // listed structurals per warp and tile (bracket kernels)
 
 __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
@@ -117,14 +119,15 @@ struct WsFront {
 	std::uint32_t ex[4];
 };
 
-// Dynamic shared memory (window addresses): [scratch, histogram][pad to 64 KiB]
-// [class table 64 KiB][ring 2 x 32 KiB].  The table and ring start on 64 KiB and
+// Dynamic shared memory (window addresses): [scratch, histogram, structural lists]
+// [pad to 64 KiB][class table 64 KiB][ring 2 x 32 KiB].  The table and ring start on 64 KiB and
 // 1 KiB boundaries of the shared window respectively.
 struct SmemWs {
 	static constexpr int kBars	   = 0;	 // full[2] tot[4] base[4]
 	static constexpr int kScratch  = 128;
 	static constexpr int kHist	   = (kScratch + static_cast<int>(sizeof(WsScratch)) + 127) & ~127;
-	static constexpr int kLowEnd   = kHist + 2 * kKeyWindow * 4;
+	static constexpr int kList	   = kHist + 2 * kKeyWindow * 4;	// per-warp structural lists
+	static constexpr int kLowEnd   = kList + kWorkers * kListCap * 2;
 	static constexpr int kTblBytes = 256 * 256;
 	static constexpr int kBytes	   = kLowEnd + 65535 + kTblBytes + 2 * kWsTile;
 };
@@ -137,27 +140,89 @@ struct OpSum3 {
 	}
 };
 
-// Inclusive warp scan of 4-lane elements; only the first NL lanes are live (the
-// others are zero on every thread, which the compiler then folds away).
-// Tag half of a tile's aggregate words: this scan's epoch (22 bits), the tile's
-// toggle parity q and a valid bit.  The epoch is never 0, so a cleared or stale
-// word never matches.
-__device__ __forceinline__ std::uint32_t agg_tag(std::uint32_t epoch, std::uint32_t q) {
-	return (epoch << 8) | (q << 1) | 1u;
+// Tag half of a tile's aggregate words: this scan's epoch (22 bits), 7 bits of the
+// tile's element (parity paths: the toggle parity q; escape path: the automaton
+// element and the first non-backslash byte's classes) and a valid bit.  The epoch is
+// never 0, so a cleared or stale word never matches.
+__device__ __forceinline__ std::uint32_t agg_tag(std::uint32_t epoch, std::uint32_t extra7) {
+	return (epoch << 8) | (extra7 << 1) | 1u;
 }
 
 __device__ __forceinline__ bool agg_valid(std::uint64_t w, std::uint32_t epoch) {
 	return static_cast<std::uint32_t>(w >> 40) == epoch && ((w >> 32) & 1u);
 }
 
-// Aggregate of a run of tiles for the bracket-less and parity paths: counts of
-// structurals (c[0], c[1]), opens (c[2], c[3]) and closes (c[4], c[5]) when the run
-// is entered outside / inside a string, and the run's toggle parity q.  (The no-
-// string path keeps plain sums in c[0], c[2], c[4].)  Counts are 32-bit: a window
-// of up to G - 1 tiles overflows the 16-bit halves of a single tile's word.
+// Escape path, one 32-byte word (bytes outside `vm` already cleared from Bk and D):
+//   esc0  bytes escaped by a backslash run inside the word, taking the word's entry
+//         as unescaped (a run reaching bit 31 escapes a byte of the next word, which
+//         the element's b bit carries);
+//   fbit  the first valid non-backslash byte;
+//   ex0   exclusive parity of the unescaped quotes (in-string bits, entry p = 0);
+//   elem  the word's automaton element: a = no non-backslash byte, b = parity of
+//         the backslash run ending at its last valid byte, q = parity of unescaped
+//         quotes, d = fbit is a quote.
+struct EscWord {
+	std::uint32_t esc0, fbit, ex0, elem;
+};
+
+__device__ __forceinline__ EscWord esc_word(std::uint32_t Bk, std::uint32_t D, std::uint32_t vm) {
+	EscWord				w;
+	const std::uint32_t runs = Bk & ~(Bk << 1);
+	const std::uint32_t ee	 = (Bk + (runs & 0x55555555u)) & ~Bk;	 // after runs starting at even bits
+	const std::uint32_t eo	 = (Bk + (runs & 0xAAAAAAAAu)) & ~Bk;	 // after runs starting at odd bits
+	w.esc0					 = (ee & 0xAAAAAAAAu) | (eo & 0x55555555u);
+	const std::uint32_t nbv	 = ~Bk & vm;
+	w.fbit					 = nbv & (0u - nbv);
+	const std::uint32_t T0	 = D & ~w.esc0;
+	w.ex0					 = prefix_xor32(T0) ^ T0;
+	w.elem					 = kIdent;
+	if (vm != 0) {
+		const int			hi = 32 - __clz(vm);
+		const std::uint32_t bt = hi >= 32 ? Bk : (Bk << (32 - hi));
+		const std::uint32_t L  = __clz(~bt);
+		w.elem = (nbv == 0 ? 1u : 0u) | ((L & 1u) << 1) | ((__popc(T0) & 1u) << 2) | ((D & w.fbit) ? 8u : 0u);
+	}
+	return w;
+}
+
+// Escape-path aggregate of a run of bytes (a word, a thread, a warp, a tile), as 4
+// lanes: [0] structural counts, [1] opens, [2] closes, each packed (H = 0) | (H = 1)
+// << 16, and [3] the automaton element (bits 0-3: a, b, q, d) | the classes of the
+// run's first non-backslash byte << 4 (structural 1, open 2, close 4).
+//   Entered in state (e, p), the run's first non-backslash byte f is selected iff
+// p = 0 (no quote can open before it; a backslash run only decides whether f is
+// escaped), and every selected byte after f depends on H = p ^ (e & d) alone, since
+// the entry e only changes whether f is escaped (d: f is a quote).  So
+//     count(e, p) = [p = 0] * class(f) + half(counts, H).
+// Composition (A then B): B is entered in H' = H ^ q_A when A has a non-backslash
+// byte (e leaves A as b_A), so B's halves swap by q_A ^ (b_A & d_B) and its f-term
+// lands in half q_A; an all-backslash A (a = 1) only shifts B's e by b_A.
+struct OpEsc {
+	__device__ __forceinline__ void operator()(const std::uint32_t (&a)[4], std::uint32_t (&b)[4]) const {
+		const std::uint32_t ea = a[3] & 0xFu, eb = b[3] & 0xFu;
+		const std::uint32_t aa = ea & 1u, ba = (ea >> 1) & 1u, qa = (ea >> 2) & 1u;
+		const std::uint32_t db = (eb >> 3) & 1u;
+		const std::uint32_t sw = (qa ^ (ba & db)) ? 0x1032u : 0x3210u;
+		const std::uint32_t fb = b[3] >> 4;
+		const std::uint32_t sh = aa ? 32u : 16u * qa;  // where B's first byte is counted
+#pragma unroll
+		for (int c = 0; c < 3; ++c) {
+			const std::uint32_t f = sh < 32 ? ((fb >> c) & 1u) << sh : 0u;
+			b[c] = a[c] + __byte_perm(b[c], 0, sw) + f;
+		}
+		b[3] = compose_fast(ea, eb) | ((aa ? fb : (a[3] >> 4)) << 4);
+	}
+};
+
+// Aggregate of a run of tiles (the fold window): per count plane its count when
+// the run is entered with H = 0 / H = 1 (c[2i], c[2i+1]); the automaton element
+// (parity paths: a = 1, q) and, on the escape path, the classes of the run's first
+// non-backslash byte.  (The no-string path keeps plain sums in c[0], c[2], c[4].)
+// Counts are 32-bit: a window of up to G - 1 tiles overflows 16-bit halves.
 struct WinElem {
 	std::uint32_t c[6] = {0, 0, 0, 0, 0, 0};
-	std::uint32_t q	   = 0;
+	std::uint32_t elem = kIdent;
+	std::uint32_t fcl  = 0;
 
 	template<int PATH, bool BR>
 	__device__ static WinElem of(const std::uint64_t (&v)[BR ? 3 : 1]) {
@@ -168,19 +233,43 @@ struct WinElem {
 			e.c[2 * c]			  = PATH == kPathNone ? x : (x & 0xFFFFu);
 			e.c[2 * c + 1]		  = PATH == kPathNone ? x : (x >> 16);
 		}
-		e.q = PATH == kPathNone ? 0u : static_cast<std::uint32_t>(v[0] >> 33) & 1u;
+		const std::uint32_t extra = static_cast<std::uint32_t>(v[0] >> 33) & 0x7Fu;
+		if (PATH == kPathEscape) {
+			e.elem = extra & 0xFu;
+			e.fcl  = extra >> 4;
+		} else if (PATH != kPathNone) {
+			e.elem = 1u | ((extra & 1u) << 2);
+		}
 		return e;
 	}
 	// this run followed by `b`
+	template<int PATH>
 	__device__ WinElem then(const WinElem& b) const {
 		WinElem r;
+		const std::uint32_t a = elem & 1u, bb = (elem >> 1) & 1u, q = (elem >> 2) & 1u;
+		const std::uint32_t sw = PATH == kPathEscape ? (q ^ (bb & (b.elem >> 3) & 1u)) : q;
 #pragma unroll
 		for (int i = 0; i < 3; ++i) {
-			r.c[2 * i]	   = c[2 * i] + (q ? b.c[2 * i + 1] : b.c[2 * i]);
-			r.c[2 * i + 1] = c[2 * i + 1] + (q ? b.c[2 * i] : b.c[2 * i + 1]);
+			r.c[2 * i]	   = c[2 * i] + (sw ? b.c[2 * i + 1] : b.c[2 * i]);
+			r.c[2 * i + 1] = c[2 * i + 1] + (sw ? b.c[2 * i] : b.c[2 * i + 1]);
+			if (PATH == kPathEscape && !a) {
+				const std::uint32_t f = (b.fcl >> i) & 1u;
+				r.c[2 * i] += q ? 0u : f;
+				r.c[2 * i + 1] += q ? f : 0u;
+			}
 		}
-		r.q = q ^ b.q;
+		r.elem = PATH == kPathNone ? kIdent : compose_fast(elem, b.elem);
+		r.fcl  = PATH == kPathEscape ? (a ? b.fcl : fcl) : 0u;
 		return r;
+	}
+	// counts of plane i when the run is entered in state s = e | p << 1
+	template<int PATH>
+	__device__ std::uint32_t count(int i, std::uint32_t s) const {
+		if (PATH == kPathNone)
+			return c[2 * i];
+		const std::uint32_t e = s & 1u, p = (s >> 1) & 1u;
+		const std::uint32_t h = p ^ (e & (elem >> 3) & 1u);
+		return (h ? c[2 * i + 1] : c[2 * i]) + ((PATH == kPathEscape && p == 0) ? ((fcl >> i) & 1u) : 0u);
 	}
 	template<bool BR>
 	__device__ WinElem shfl_down(int off) const {
@@ -188,7 +277,9 @@ struct WinElem {
 		const int n = BR ? 6 : 2;
 #pragma unroll
 		for (int i = 0; i < 6; ++i) r.c[i] = i < n ? __shfl_down_sync(kFull, c[i], off) : 0u;
-		r.q = __shfl_down_sync(kFull, q, off);
+		r.elem = __shfl_down_sync(kFull, elem | (fcl << 4), off);
+		r.fcl  = r.elem >> 4;
+		r.elem &= 0xFu;
 		return r;
 	}
 	template<bool BR>
@@ -197,11 +288,15 @@ struct WinElem {
 		const int n = BR ? 6 : 2;
 #pragma unroll
 		for (int i = 0; i < 6; ++i) r.c[i] = i < n ? __shfl_sync(kFull, c[i], 0) : 0u;
-		r.q = __shfl_sync(kFull, q, 0);
+		r.elem = __shfl_sync(kFull, elem | (fcl << 4), 0);
+		r.fcl  = r.elem >> 4;
+		r.elem &= 0xFu;
 		return r;
 	}
 };
 
+// Inclusive warp scan of 4-lane elements; only the first NL lanes are live (the
+// others are zero on every thread, which the compiler then folds away).
 template<int NL, class Op>
 __device__ __forceinline__ void warp_scan(std::uint32_t (&x)[4], Op op, int lane, int n_active) {
 #pragma unroll
@@ -233,6 +328,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	std::uint64_t* base_bar = full_bar + 2 + kBufs;
 	WsScratch&	   sc		= *reinterpret_cast<WsScratch*>(smem + SmemWs::kScratch);
 	unsigned int*  khist	= reinterpret_cast<unsigned int*>(smem + SmemWs::kHist);
+	std::uint16_t* list_all = reinterpret_cast<std::uint16_t*>(smem + SmemWs::kList);
 	const std::uint32_t win0	= smem_addr(smem);
 	const std::uint32_t tbl_win = (win0 + SmemWs::kLowEnd + 0xFFFFu) & ~0xFFFFu;
 	std::uint32_t*		tbl		= reinterpret_cast<std::uint32_t*>(smem + (tbl_win - win0));
@@ -240,6 +336,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 
 	const int			tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	constexpr int		NL	= BR ? 4 : 2;  // live element lanes: S counts, parity (, O, C)
+	constexpr int		NE	= PATH == kPathEscape ? 4 : NL;	 // lanes handed between warps
 	const DevPlan*		P	= a.plan;
 	DevResult*			res = a.res;
 	std::uint64_t*		d_agg  = static_cast<std::uint64_t*>(a.tiles);	// [3][ntiles]
@@ -279,8 +376,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 	const std::uint32_t n_mine	 = my_first < ntiles ? (ntiles - 1 - my_first) / G + 1 : 0u;
 	auto tile_of = [&](std::uint32_t k) { return my_first + k * G; };
 
-	long long ext_min_bal = 0, ext_max_bal = 0;
-	long long ext_min_key = 0x7FFFFFFFFFFFFFFFll, ext_max_key = -0x7FFFFFFFFFFFFFFFll;
+	// depth extrema of this thread's brackets: balance after each bracket, and keys
+	int ext_min_bal = 0, ext_max_bal = 0;
+	int ext_min_key = 0x7FFFFFFF, ext_max_key = -0x7FFFFFFF;
 	bool	  any_keys = false;
 
 	if (warp == kMgr) {
@@ -301,31 +399,38 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			std::uint32_t w[4] = {0, 0, 0, 0};
 			if (lane < kWorkers)
 #pragma unroll
-				for (int i = 0; i < NL; ++i) w[i] = sc.wtot[buf][lane][i];
+				for (int i = 0; i < NE; ++i) w[i] = sc.wtot[buf][lane][i];
+			if (PATH == kPathEscape && lane >= kWorkers)
+				w[3] = kIdent;
 			if (PATH == kPathNone)
 				warp_scan<NL>(w, OpSum3(), lane, kWorkers);
+			else if (PATH == kPathEscape)
+				warp_scan<4>(w, OpEsc(), lane, kWorkers);
 			else
 				warp_scan<NL>(w, OpParity(), lane, kWorkers);
 			std::uint32_t we[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < NL; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
+			for (int i = 0; i < NE; ++i) we[i] = __shfl_up_sync(kFull, w[i], 1);
 			if (lane == 0)
 #pragma unroll
-				for (int i = 0; i < 4; ++i) we[i] = 0;
+				for (int i = 0; i < 4; ++i) we[i] = (PATH == kPathEscape && i == 3) ? kIdent : 0u;
 			if (lane < kWorkers)
 #pragma unroll
-				for (int i = 0; i < NL; ++i) sc.wpre[buf][lane][i] = we[i];
+				for (int i = 0; i < NE; ++i) sc.wpre[buf][lane][i] = we[i];
 			std::uint32_t tot[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < NL; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
-			// AGG payload: packed counts; for the parity paths the tile element (a=1, q)
-			const uint4 agg = PATH == kPathNone ? make_uint4(tot[0], tot[2], tot[3], 0u)
-												: make_uint4(tot[0], tot[2], tot[3], 1u | ((tot[1] & 1u) << 2));
+			for (int i = 0; i < NE; ++i) tot[i] = __shfl_sync(kFull, w[i], kWorkers - 1);
+			// AGG payload: packed counts; the tile element (parity paths: a = 1, q;
+			// escape path: element | first-byte classes << 4)
+			const uint4 agg = PATH == kPathNone	  ? make_uint4(tot[0], tot[2], tot[3], 0u)
+							: PATH == kPathEscape ? make_uint4(tot[0], tot[1], tot[2], tot[3])
+												  : make_uint4(tot[0], tot[2], tot[3], 1u | ((tot[1] & 1u) << 2));
 			if (lane == 0) {
 				sc.tagg[buf] = agg;
 				// one self-validating 64-bit word per count plane: a reader that sees
 				// this scan's tag sees the payload stored with it
-				const std::uint64_t tag = static_cast<std::uint64_t>(agg_tag(epoch, (agg.w >> 2) & 1u)) << 32;
+				const std::uint32_t extra = PATH == kPathEscape ? (agg.w & 0x7Fu) : ((agg.w >> 2) & 1u);
+				const std::uint64_t tag	  = static_cast<std::uint64_t>(agg_tag(epoch, extra)) << 32;
 				st_relaxed64(&d_agg[t], tag | agg.x);
 				if (BR) {
 					st_relaxed64(&d_agg[ntiles + t], tag | agg.y);
@@ -391,20 +496,19 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
 					for (int i = kLB - 1; i >= 0; --i)
 						if (static_cast<std::uint32_t>(lane) * kLB + i < nwin)
-							r = r.then(WinElem::of<PATH, BR>(lbv[i]));
+							r = r.template then<PATH>(WinElem::of<PATH, BR>(lbv[i]));
 					// suffix scan over the lanes: lane 0 ends with the whole window
 #pragma unroll
 					for (int off = 1; off < 32; off <<= 1) {
 						const WinElem o = r.shfl_down<BR>(off);
 						if (lane + off < 32)
-							r = o.then(r);
+							r = o.template then<PATH>(r);
 					}
 					r = r.shfl0<BR>();
-					const std::uint32_t p_prev = (s_prev >> 1) & 1u;
-					s_t		= PATH == kPathNone ? 0u : (s_prev ^ (r.q << 1));
-					base[0] = base_prev[0] + (p_prev ? r.c[1] : r.c[0]);
-					base[1] = base_prev[1] + (p_prev ? r.c[3] : r.c[2]);
-					base[2] = base_prev[2] + (p_prev ? r.c[5] : r.c[4]);
+					s_t		= PATH == kPathNone ? 0u : apply_fast(r.elem, s_prev);
+					base[0] = base_prev[0] + r.template count<PATH>(0, s_prev);
+					base[1] = base_prev[1] + r.template count<PATH>(1, s_prev);
+					base[2] = base_prev[2] + r.template count<PATH>(2, s_prev);
 					std::uint32_t c0, c1, c2;
 					agg_counts<PATH>(agg, s_t, c0, c1, c2);
 					s_prev		 = PATH == kPathNone ? 0u : apply_fast(agg.w & 0xFu, s_t);
@@ -457,9 +561,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 		for (int c = 0; c < 4; ++c)
 			chunk_off[c] = row * 128u + ((((half << 2) + c) ^ (row & 7u)) << 4);
 		const std::uint8_t	delim	   = P->delim;
+		const std::uint32_t esc_rep	   = P->escape_rep;
 		const bool			want_pairs = (a.flags & 1u) != 0;
 		const bool			want_chars = (a.flags & 4u) != 0;
 		const bool			want_mask  = (a.flags & 8u) != 0 && a.mask;
+		const bool			own_bchar  = (a.flags & kScanOwnBchar) != 0;
 		const std::uint32_t cap_s = a.cap_s > 0xFFFFFFFFull ? 0xFFFFFFFFu : static_cast<std::uint32_t>(a.cap_s);
 		const std::uint32_t cap_b = a.cap_b > 0xFFFFFFFFull ? 0xFFFFFFFFu : static_cast<std::uint32_t>(a.cap_b);
 
@@ -591,6 +697,22 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 					e[1]   = 0;
 					e[2]   = BR ? __popc(O) : 0u;
 					e[3]   = BR ? __popc(C) : 0u;
+				} else if (PATH == kPathEscape) {
+					// counts of the bytes after the first non-backslash byte, by H
+					std::uint32_t Bk = eq_mask32(r, esc_rep);
+					if (!interior)
+						Bk &= vm;
+					F.dd[h]					  = Bk;	 // the escape path keeps its backslashes here
+					const EscWord		W	  = esc_word(Bk, D, vm);
+					const std::uint32_t above = W.fbit ? ~((W.fbit << 1) - 1u) : 0u;
+					const std::uint32_t in0 = above & ~W.ex0, in1 = above & W.ex0;
+					ex0[h]					= 0;
+					e[0]					= __popc(S & in0) | (__popc(S & in1) << 16);
+					e[1]					= BR ? (__popc(O & in0) | (__popc(O & in1) << 16)) : 0u;
+					e[2]					= BR ? (__popc(C & in0) | (__popc(C & in1) << 16)) : 0u;
+					const std::uint32_t fcl = ((S & W.fbit) ? 1u : 0u) | ((O & W.fbit) ? 2u : 0u)
+											| ((C & W.fbit) ? 4u : 0u);
+					e[3] = W.elem | ((BR ? fcl : (fcl & 1u)) << 4);
 				} else {
 					ex0[h] = prefix_xor32(D) ^ D;
 					e[0]   = 0;
@@ -604,8 +726,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
 					for (int i = 0; i < 4; ++i) v[i] = e[i];
 			}
-			F.dd[0] = F.dd[1] = 0;
-			if (PATH == kPathParity || PATH == kPathDoubled) {
+			if (PATH != kPathEscape)
+				F.dd[0] = F.dd[1] = 0;
+			if (PATH == kPathEscape) {
+				OpEsc()(w0, v);	 // thread element = word 0 then word 1
+			} else if (PATH == kPathParity || PATH == kPathDoubled) {
 				if (PATH == kPathDoubled) {
 					// previous-byte-delimiter bits: word 1 takes word 0's last byte; word 0
 					// takes the previous thread's last byte (lane - 1, or memory for lane 0)
@@ -648,22 +773,24 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				F.sel0[1] = F.sel1[1] = F.S[1];
 				OpSum3()(w0, v);
 			}
-			if (!BR)
+			if (!BR && PATH != kPathEscape)
 				v[2] = v[3] = 0;
 			if (PATH == kPathNone)
 				warp_scan<NL>(v, OpSum3(), lane, 32);
+			else if (PATH == kPathEscape)
+				warp_scan<4>(v, OpEsc(), lane, 32);
 			else
 				warp_scan<NL>(v, OpParity(), lane, 32);
 #pragma unroll
 			for (int i = 0; i < 4; ++i) {
-				const std::uint32_t e = i < NL ? __shfl_up_sync(kFull, v[i], 1) : 0u;
-				F.ex[i]				  = lane == 0 ? 0u : e;
+				const std::uint32_t e = i < NE ? __shfl_up_sync(kFull, v[i], 1) : 0u;
+				F.ex[i]				  = lane == 0 ? ((PATH == kPathEscape && i == 3) ? kIdent : 0u) : e;
 			}
 			if (!BR && PATH != kPathNone)
 				F.ex[1] |= (w0[1] & 1u) << 1;
 			if (lane == 31)
 #pragma unroll
-				for (int i = 0; i < NL; ++i) sc.wtot[buf][warp][i] = v[i];
+				for (int i = 0; i < NE; ++i) sc.wtot[buf][warp][i] = v[i];
 			__syncwarp();
 			if (lane == 0)
 				mbar_arrive(&tot_bar[buf]);
@@ -692,19 +819,29 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			const std::uint32_t		 p_t = (s_t >> 1) & 1u;
 			std::uint32_t			 pre[4] = {0, 0, 0, 0};
 #pragma unroll
-			for (int i = 0; i < NL; ++i) pre[i] = sc.wpre[buf][warp][i];
+			for (int i = 0; i < NE; ++i) pre[i] = sc.wpre[buf][warp][i];
 			const std::uint32_t base[3] = {sc.base[buf][0], sc.base[buf][1], sc.base[buf][2]};
 			// prefix of word 0: the warp's prefix, then this thread's warp-exclusive prefix
 			std::uint32_t p0[4] = {F.ex[0], F.ex[1], F.ex[2], F.ex[3]};
 			if (PATH == kPathNone)
 				OpSum3()(pre, p0);
+			else if (PATH == kPathEscape)
+				OpEsc()(pre, p0);
 			else
 				OpParity()(pre, p0);
-			std::uint32_t off[3], p_w = 0;
+			std::uint32_t off[3], p_w = 0, s_w = 0;
 			if (PATH == kPathNone) {
 				off[0] = p0[0];
 				off[1] = p0[2];
 				off[2] = p0[3];
+			} else if (PATH == kPathEscape) {
+				// counts before this thread's bytes, and the state entering them
+				const std::uint32_t e_t = s_t & 1u;
+				const std::uint32_t h_t = p_t ^ (e_t & (p0[3] >> 3) & 1u);
+				const std::uint32_t fc	= (p0[3] >> 4) & 7u;
+#pragma unroll
+				for (int c = 0; c < 3; ++c) off[c] = half16(p0[c], h_t) + (p_t == 0 ? ((fc >> c) & 1u) : 0u);
+				s_w = apply_fast(p0[3] & 0xFu, s_t);
 			} else {
 				p_w	   = p_t ^ (p0[1] & 1u);
 				off[0] = half16(p0[0], p_t);
@@ -713,7 +850,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			}
 			const bool interior = static_cast<unsigned long long>(t) * kWsTile >= a.o
 							   && static_cast<unsigned long long>(t + 1) * kWsTile <= doc_end;
-			if constexpr (!BR) {
+			if constexpr (!BR && PATH != kPathEscape) {
 				// bracket-less: pick each word's selection by its entry parity
 				std::uint32_t si = base[0] + off[0];
 #pragma unroll
@@ -751,112 +888,204 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 				}
 				return true;
 			} else {
+				// masks of both words (and the per-word bookkeeping) first, outputs after
+				std::uint32_t sel[2], so[2], scl[2];
 #pragma unroll
-			for (int h = 0; h < 2; ++h) {
-				const unsigned long long qw = q0 + 32u * h;
-				const std::uint32_t		 vm = valid_mask(qw, interior);
-				std::uint32_t			 mask = 0;
-				if (PATH != kPathNone) {
-					const std::uint32_t ex0 = prefix_xor32(F.D[h]) ^ F.D[h];
-					mask = ((ex0 ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd[h]) & vm;
-				}
-				if (vm != 0 && doc_end <= qw + 32 && doc_end > qw) {
-					const int			hi		  = static_cast<int>(doc_end - qw);
-					const std::uint32_t elem	  = 1u | ((__popc(F.D[h]) & 1u) << 2);
-					const std::uint32_t endstate  = PATH == kPathNone ? 0u : apply_fast(elem, p_w << 1);
-					const std::uint32_t last_flag = PATH == kPathNone ? 0u : (F.D[h] >> (hi - 1)) & 1u;
-					const std::uint32_t unclosed  = PATH == kPathNone ? 0u : (((endstate >> 1) & 1u) | last_flag);
-					res->unclosed				  = unclosed;
-					if (a.carry_out) {
-						a.carry_out->fstate		 = endstate;
-						a.carry_out->last_delim	 = last_flag;
-						a.carry_out->last_toggle = last_flag;
-						a.carry_out->unclosed	 = unclosed;
+				for (int h = 0; h < 2; ++h) {
+					const unsigned long long qw = q0 + 32u * h;
+					const std::uint32_t		 vm = valid_mask(qw, interior);
+					std::uint32_t			 mask = 0, esc = 0, welem = 0;
+					if (PATH == kPathEscape) {
+						// the word's exact entry state resolves the first byte's escape
+						const EscWord		W	  = esc_word(F.dd[h], F.D[h], vm);
+						const std::uint32_t e_w	  = s_w & 1u, pw = (s_w >> 1) & 1u;
+						const std::uint32_t above = W.fbit ? ~((W.fbit << 1) - 1u) : 0u;
+						const std::uint32_t exw	  = W.ex0 ^ ((e_w && (F.D[h] & W.fbit)) ? above : 0u);
+						mask					  = (exw ^ (pw ? 0xFFFFFFFFu : 0u)) & vm;
+						esc						  = W.esc0 ^ (e_w ? W.fbit : 0u);
+						welem					  = W.elem;
+						// an escaped quote outside a string: the descriptor would toggle there
+						// (a backslash outside strings is inert); the host reruns this input
+						// on the general kernel
+						if (F.D[h] & esc & ~mask)
+							atomicOr(&res->spec_fail, 1u);
+					} else if (PATH != kPathNone) {
+						const std::uint32_t ex0 = prefix_xor32(F.D[h]) ^ F.D[h];
+						mask = ((ex0 ^ (p_w ? 0xFFFFFFFFu : 0u)) | F.dd[h]) & vm;
 					}
-				}
-				std::uint32_t		m	 = F.S[h] & ~mask;
-				std::uint32_t		si	 = base[0] + off[0];
-				const std::uint32_t no0	 = base[1] + off[1];
-				const std::uint32_t nc0	 = base[2] + off[2];
-				const std::uint32_t pos0 = byte_base + static_cast<std::uint32_t>(qw - a.o);
-				const unsigned char* gb	 = a.base + qw;	 // input bytes (global, L2-resident)
-				if (h == 0) {
-					// word 1 starts after word 0's selected bytes and toggles
-					off[0] += __popc(m);
-					if (BR) {
-						off[1] += __popc(F.O[0] & ~mask);
-						off[2] += __popc(F.C[0] & ~mask);
-					}
-					if (PATH != kPathNone)
-						p_w ^= __popc(F.D[0]) & 1u;
-				}
-				if (!BR) {
-					if (si + static_cast<std::uint32_t>(__popc(m)) <= cap_s && !want_chars && !want_pairs) {
-						std::uint32_t* out = a.pos + si;
-						while (m) {
-							const int j = __ffs(m) - 1;
-							m &= m - 1;
-							*out++ = pos0 + j;
+					if (vm != 0 && doc_end <= qw + 32 && doc_end > qw) {
+						const int	  hi = static_cast<int>(doc_end - qw);
+						std::uint32_t endstate = 0, last_flag = 0, last_delim = 0;
+						if (PATH == kPathEscape) {
+							endstate   = apply_fast(welem, s_w);
+							last_flag  = ((F.D[h] & ~esc) >> (hi - 1)) & 1u;
+							last_delim = (F.D[h] >> (hi - 1)) & 1u;
+						} else if (PATH != kPathNone) {
+							const std::uint32_t elem = 1u | ((__popc(F.D[h]) & 1u) << 2);
+							endstate				 = apply_fast(elem, p_w << 1);
+							last_flag = last_delim = (F.D[h] >> (hi - 1)) & 1u;
 						}
-					} else {
+						const std::uint32_t unclosed = PATH == kPathNone ? 0u : (((endstate >> 1) & 1u) | last_flag);
+						res->unclosed				 = unclosed;
+						if (a.carry_out) {
+							a.carry_out->fstate		 = endstate;
+							a.carry_out->last_delim	 = last_delim;
+							a.carry_out->last_toggle = last_flag;
+							a.carry_out->unclosed	 = unclosed;
+						}
+					}
+					sel[h] = F.S[h] & ~mask;
+					so[h]  = BR ? (F.O[h] & ~mask) : 0u;
+					scl[h] = BR ? (F.C[h] & ~mask) : 0u;
+					if (h == 0) {
+						// word 1 starts after word 0's toggles
+						if (PATH == kPathEscape)
+							s_w = apply_fast(welem, s_w);
+						else if (PATH != kPathNone)
+							p_w ^= __popc(F.D[0]) & 1u;
+					}
+					if (want_mask && vm != 0)
+						a.mask[(byte_base + static_cast<std::uint32_t>(qw - a.o)) >> 5] = mask;
+				}
+
+				// The warp's structurals are one run of the output, in byte order.  List
+				// them in shared memory (a cheap divergent loop), then handle the list 32
+				// at a time with every lane busy: structural and bracket indices and depths
+				// follow from ballots, and the stores land on consecutive indices.
+				const std::uint32_t cnt = __popc(sel[0]) + __popc(sel[1]);
+				std::uint32_t		incl = cnt;
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const std::uint32_t y = __shfl_up_sync(kFull, incl, o);
+					if (lane >= o)
+						incl += y;
+				}
+				const std::uint32_t total = __shfl_sync(kFull, incl, 31);
+				if (total <= static_cast<std::uint32_t>(kListCap)) {
+					std::uint16_t* L = list_all + warp * kListCap;
+					std::uint32_t  o = incl - cnt;
+#pragma unroll
+					for (int h = 0; h < 2; ++h) {
+						std::uint32_t m = sel[h];
 						while (m) {
 							const int j = __ffs(m) - 1;
 							m &= m - 1;
+							L[o++] = static_cast<std::uint16_t>(j | (h << 5) | (lane << 6) | (((so[h] >> j) & 1u) << 11)
+																| (((scl[h] >> j) & 1u) << 12));
+						}
+					}
+					__syncwarp();
+					const std::uint32_t si0	 = __shfl_sync(kFull, base[0] + off[0], 0);
+					const std::uint32_t no0	 = __shfl_sync(kFull, base[1] + off[1], 0);
+					const std::uint32_t nc0	 = __shfl_sync(kFull, base[2] + off[2], 0);
+					const std::uint32_t lt	 = (1u << lane) - 1u;
+					const unsigned long long wq0 = static_cast<unsigned long long>(t) * kWsTile + 64ull * (warp * 32u);
+					std::uint32_t		nop = 0, ncl = 0;  // brackets of earlier rounds
+					for (std::uint32_t r0 = 0; r0 < total; r0 += 32) {
+						const std::uint32_t i	  = r0 + static_cast<std::uint32_t>(lane);
+						const bool			valid = i < total;
+						const std::uint32_t code  = valid ? L[i] : 0u;
+						const bool			isop  = BR && valid && ((code >> 11) & 1u);
+						const bool			iscl  = BR && valid && ((code >> 12) & 1u);
+						const std::uint32_t bo = BR ? __ballot_sync(kFull, isop) : 0u;
+						const std::uint32_t bc = BR ? __ballot_sync(kFull, iscl) : 0u;
+						if (valid) {
+							const unsigned long long q =
+								wq0 + 64u * ((code >> 6) & 31u) + 32u * ((code >> 5) & 1u) + (code & 31u);
+							const std::uint32_t pos = byte_base + static_cast<std::uint32_t>(q - a.o);
+							const std::uint32_t si	= si0 + i;
 							if (si < cap_s) {
-								a.pos[si] = pos0 + j;
+								a.pos[si] = pos;
+								if (want_chars)
+									a.chars[si] = a.base[q];
+								if (want_pairs)
+									a.pair[si] = -1;
+							}
+							if (BR && (isop || iscl)) {
+								const std::uint32_t ob	= nop + __popc(bo & lt), cb = ncl + __popc(bc & lt);
+								const std::uint32_t bi	= no0 + nc0 + ob + cb;
+								const int			dep = static_cast<int>((no0 + ob) - (nc0 + cb));
+								const int			key = isop ? dep : dep - 1;
+								const int			aft = isop ? dep + 1 : dep - 1;
+								if (bi < cap_b) {
+									a.bpos[bi] = pos;
+									if (own_bchar)
+										a.bchar[bi] = a.base[q];
+									a.bsi[bi]	= si;
+									a.depth[bi] = key;
+								}
+								ext_min_bal = aft < ext_min_bal ? aft : ext_min_bal;
+								ext_max_bal = aft > ext_max_bal ? aft : ext_max_bal;
+								ext_min_key = key < ext_min_key ? key : ext_min_key;
+								ext_max_key = key > ext_max_key ? key : ext_max_key;
+								any_keys	= true;
+								if (key >= -kKeyWindow && key < kKeyWindow)
+									atomicAdd(&khist[key + kKeyWindow], 1u);
+								else
+									atomicOr(&res->keys_oob, 1u);
+							}
+						}
+						nop += __popc(bo);
+						ncl += __popc(bc);
+					}
+					__syncwarp();
+				} else {
+					// a dense warp: each thread writes its own structurals
+#pragma unroll
+					for (int h = 0; h < 2; ++h) {
+						const unsigned long long qw	  = q0 + 32u * h;
+						std::uint32_t			 m	  = sel[h];
+						std::uint32_t			 si	  = base[0] + off[0];
+						const std::uint32_t		 no0  = base[1] + off[1];
+						const std::uint32_t		 nc0  = base[2] + off[2];
+						const std::uint32_t		 pw0  = byte_base + static_cast<std::uint32_t>(qw - a.o);
+						const unsigned char*	 gb	  = a.base + qw;
+						std::uint32_t			 bi	  = no0 + nc0;
+						int						 dep  = static_cast<int>(no0 - nc0);
+						const std::uint32_t		 bm	  = so[h] | scl[h];
+						if (h == 0) {
+							off[0] += __popc(m);
+							off[1] += __popc(so[0]);
+							off[2] += __popc(scl[0]);
+						}
+						while (m) {
+							const int j = __ffs(m) - 1;
+							m &= m - 1;
+							const std::uint32_t pos = pw0 + j;
+							if (si < cap_s) {
+								a.pos[si] = pos;
 								if (want_chars)
 									a.chars[si] = gb[j];
 								if (want_pairs)
 									a.pair[si] = -1;
 							}
+							if (BR && ((bm >> j) & 1u)) {
+								const bool op  = (so[h] >> j) & 1u;
+								const int  key = op ? dep : dep - 1;
+								dep += op ? 1 : -1;
+								if (bi < cap_b) {
+									a.bpos[bi] = pos;
+									if (own_bchar)
+										a.bchar[bi] = gb[j];
+									a.bsi[bi]	= si;
+									a.depth[bi] = key;
+								}
+								++bi;
+								ext_min_bal = dep < ext_min_bal ? dep : ext_min_bal;
+								ext_max_bal = dep > ext_max_bal ? dep : ext_max_bal;
+								ext_min_key = key < ext_min_key ? key : ext_min_key;
+								ext_max_key = key > ext_max_key ? key : ext_max_key;
+								any_keys	= true;
+								if (key >= -kKeyWindow && key < kKeyWindow)
+									atomicAdd(&khist[key + kKeyWindow], 1u);
+								else
+									atomicOr(&res->keys_oob, 1u);
+							}
 							++si;
 						}
 					}
-				} else {
-					const std::uint32_t selo = F.O[h] & ~mask;
-					const std::uint32_t selc = F.C[h] & ~mask;
-					std::uint32_t		bi	 = no0 + nc0;
-					long long			dep	 = static_cast<long long>(no0) - static_cast<long long>(nc0);
-					const std::uint32_t bm	 = selo | selc;
-					while (m) {
-						const int j = __ffs(m) - 1;
-						m &= m - 1;
-						const std::uint32_t pos = pos0 + j;
-						if (si < cap_s) {
-							a.pos[si] = pos;
-							if (want_chars)
-								a.chars[si] = gb[j];
-							if (want_pairs)
-								a.pair[si] = -1;
-						}
-						if ((bm >> j) & 1u) {
-							const bool		op	= (selo >> j) & 1u;
-							const long long key = op ? dep : dep - 1;
-							dep += op ? 1 : -1;
-							if (bi < cap_b) {
-								a.bpos[bi]	= pos;
-								a.bchar[bi] = gb[j];
-								a.bsi[bi]	= si;
-								a.depth[bi] = static_cast<std::int32_t>(key);
-							}
-							++bi;
-							ext_min_bal = dep < ext_min_bal ? dep : ext_min_bal;
-							ext_max_bal = dep > ext_max_bal ? dep : ext_max_bal;
-							ext_min_key = key < ext_min_key ? key : ext_min_key;
-							ext_max_key = key > ext_max_key ? key : ext_max_key;
-							any_keys	= true;
-							if (key >= -kKeyWindow && key < kKeyWindow)
-								atomicAdd(&khist[key + kKeyWindow], 1u);
-							else
-								atomicOr(&res->keys_oob, 1u);
-						}
-						++si;
-					}
 				}
-				if (want_mask && vm != 0)
-					a.mask[(byte_base + static_cast<std::uint32_t>(qw - a.o)) >> 5] = mask;
-			}
-			return true;
+				return true;
 			}
 		};
 
@@ -889,7 +1118,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			sc.any_br = 0;
 		__syncthreads();
 		if (warp < kWorkers) {
-			const long long v0 = warp_min(ext_min_bal), v1 = warp_max(ext_max_bal);
+			const long long v0 = warp_min(static_cast<long long>(ext_min_bal)),
+							v1 = warp_max(static_cast<long long>(ext_max_bal));
 			const long long v2 = warp_min(ext_min_key), v3 = warp_max(ext_max_key);
 			const bool		anyk = __any_sync(kFull, any_keys);
 			if (lane == 0) {
@@ -930,6 +1160,8 @@ PARS_INST(kPathParity, false)
 PARS_INST(kPathParity, true)
 PARS_INST(kPathDoubled, false)
 PARS_INST(kPathDoubled, true)
+PARS_INST(kPathEscape, false)
+PARS_INST(kPathEscape, true)
 #undef PARS_INST
 
 int scan_ws_threads() {
@@ -952,6 +1184,8 @@ const void* scan_ws_kernel(int path, bool brackets) {
 		case 3: return reinterpret_cast<const void*>(&k_scan_ws<kPathParity, true>);
 		case 4: return reinterpret_cast<const void*>(&k_scan_ws<kPathDoubled, false>);
 		case 5: return reinterpret_cast<const void*>(&k_scan_ws<kPathDoubled, true>);
+		case 6: return reinterpret_cast<const void*>(&k_scan_ws<kPathEscape, false>);
+		case 7: return reinterpret_cast<const void*>(&k_scan_ws<kPathEscape, true>);
 		default: return nullptr;
 	}
 }
