@@ -161,6 +161,48 @@ int pars_scan_chunk(pars_ctx* ctx, int plan_id, const uint8_t* d_chunk, uint64_t
 int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
                       uint32_t flags, void* stream, pars_device_result* out);
 
+/* ---- batched documents ---------------------------------------------------- */
+/* No counterpart in the reference (its scanner takes one document per call).  Many
+ * documents, concatenated in device memory, in one persistent launch: each CTA scans
+ * whole documents (largest first), the scan state resets at every document start,
+ * and R6 pairs every document's brackets in one sort keyed by (document, depth).
+ * Each document's results are exactly those of pars_scan_device on it alone.
+ * Documents the fast kernel cannot finish on its own (an escaped quote outside a
+ * string, depth keys beyond +-1024, an output region too small) and plans without a
+ * fast path are recomputed one by one inside the call (n_recomputed counts them).
+ * Blocks until the results are ready; pointers stay valid until the next batch
+ * call on the context. */
+typedef struct pars_batch_result {
+  uint32_t ndocs;
+  uint32_t grid;                 /* CTAs of the persistent launch                      */
+  uint32_t n_recomputed;
+  uint32_t reserved;
+  /* document d: structural[struct_off[d] .. struct_off[d] + n_struct[d]), byte
+   * offsets relative to the document's start; pair_pos (PARS_WANT_PAIRS) and chars
+   * (PARS_WANT_CHARS) use the same indexing, pair_pos in the document's own
+   * structural-index space (-1 if none). */
+  const uint32_t* structural;
+  const int32_t* pair_pos;
+  const uint8_t* chars;
+  const uint32_t* struct_off;    /* [ndocs] */
+  const uint32_t* n_struct;      /* [ndocs] */
+  /* brackets of document d: bracket_pos / depth [bracket_off[d] .. + n_brackets[d]) */
+  const uint32_t* bracket_pos;
+  const int32_t* depth;
+  const uint32_t* bracket_off;   /* [ndocs] */
+  const uint32_t* n_brackets;    /* [ndocs] */
+  const int32_t* unclosed_mode;  /* [ndocs] */
+  const int32_t* balanced;       /* [ndocs] with PARS_RUN_PAIRS, else NULL */
+  const int32_t* well_formed;
+  const int32_t* max_depth;
+} pars_batch_result;
+
+/* d_in: the concatenated documents (device memory); offsets (host memory, ndocs + 1
+ * entries, offsets[0] = 0): document d is d_in[offsets[d] .. offsets[d + 1]).
+ * At most 2^20 documents, each < 2^32 bytes.  PARS_WANT_MASK is not supported. */
+int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, const uint64_t* offsets,
+                    uint32_t ndocs, uint32_t flags, void* stream, pars_batch_result* out);
+
 /* ---- scan without allocation ---------------------------------------------- */
 /* No counterpart in the reference (whose scanner always owns a DeviceCache that
  * grows with cudaMalloc, pipeline.cuh:562-714).  For callers that must not allocate

@@ -66,6 +66,19 @@ class NoAllocResult(ctypes.Structure):
 PARS_NOALLOC_MAX_BYTES = 134217728
 
 
+class BatchResult(ctypes.Structure):
+    """pars_batch_result: device pointers, per-document arrays of `ndocs` entries."""
+    _fields_ = [("ndocs", ctypes.c_uint32), ("grid", ctypes.c_uint32),
+                ("n_recomputed", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("structural", ctypes.c_void_p), ("pair_pos", ctypes.c_void_p),
+                ("chars", ctypes.c_void_p), ("struct_off", ctypes.c_void_p),
+                ("n_struct", ctypes.c_void_p), ("bracket_pos", ctypes.c_void_p),
+                ("depth", ctypes.c_void_p), ("bracket_off", ctypes.c_void_p),
+                ("n_brackets", ctypes.c_void_p), ("unclosed_mode", ctypes.c_void_p),
+                ("balanced", ctypes.c_void_p), ("well_formed", ctypes.c_void_p),
+                ("max_depth", ctypes.c_void_p)]
+
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "pars_version": (ctypes.c_int, []),
@@ -93,6 +106,10 @@ SIGNATURES = {
     "pars_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                         ctypes.POINTER(ctypes.c_float)]),
     "pars_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "pars_scan_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_void_p,
+                                       ctypes.POINTER(BatchResult)]),
     "pars_scan_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.c_void_p, ctypes.c_void_p]),

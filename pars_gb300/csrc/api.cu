@@ -14,6 +14,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
+#include <numeric>
+#include <queue>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -26,20 +29,20 @@
 
 namespace pars {
 
-// kernels (scan_fast.cu / scan.cu / pair.cu)
+// kernels (scan_ws.cu / scan.cu / pair.cu)
 int		   scan_smem_bytes(int path);
 const void* scan_kernel(int path);
-int		   scan_fast_smem_bytes();
-int		   scan_fast_max_grid();
+int		   scan_ws_max_grid();
 int		   scan_ws_threads();
 int		   scan_ws_tile_bytes();
 struct WsArgs {
 	ScanArgs		   a;
 	unsigned long long rows_full;
+	BatchDesc		   bd;
 };
+const void* scan_ws_batch_kernel(int path, bool brackets);
 int		   scan_ws_smem_bytes();
 const void* scan_ws_kernel(int path, bool brackets);
-const void* scan_fast_kernel(int path, bool brackets);
 int		   sort_tile_keys();
 const void* bchar_gather_kernel();
 struct SortPass;
@@ -126,6 +129,17 @@ struct pars_ctx {
 	uint64_t	launches   = 0;
 	// the document of the current whole-document scan (R6 gathers bracket bytes)
 	const uint8_t* cur_in = nullptr;
+	// batched documents (pars_scan_batch)
+	struct Batch {
+		DevBuf doc_start, items, item_begin, region_s, region_b, doc_cta;
+		DevBuf sbase, bbase, nstruct, nopen, nclose, nbr, unclosed, minbal, maxbal, flags, cbase, seg;
+		DevBuf balanced, well_formed, max_depth, cta_bcount, bdoc;
+		DevBuf dpos, dsi, ddepth, dkey, dkey_b, order_b, order;
+		DevResult* bres = nullptr;
+		int		   blocks[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+		pars_ctx*  helper = nullptr;  // recomputes flagged documents on their own
+		std::vector<uint32_t> h_flags;
+	} batch;
 };
 
 namespace {
@@ -361,7 +375,7 @@ bool use_ws(int path) {
 }
 
 const void* fast_kernel(int path, bool br) {
-	return use_ws(path) ? scan_ws_kernel(path, br) : scan_fast_kernel(path, br);
+	return use_ws(path) ? scan_ws_kernel(path, br) : nullptr;
 }
 
 int fast_threads(int path) {
@@ -369,7 +383,7 @@ int fast_threads(int path) {
 }
 
 int fast_smem(int path) {
-	return use_ws(path) ? scan_ws_smem_bytes() : scan_fast_smem_bytes();
+	return use_ws(path) ? scan_ws_smem_bytes() : 0;
 }
 
 int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
@@ -384,7 +398,7 @@ int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "fast scan kernel does not fit on an SM");
 	// the look-back window of a tile spans one wave (G tiles), held by one warp
-	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, scan_fast_max_grid());
+	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, scan_ws_max_grid());
 	return 0;
 }
 
@@ -840,6 +854,19 @@ int pars_destroy(pars_ctx* ctx) {
 					  &ctx->bsi, &ctx->depth, &ctx->bpair, &ctx->order, &ctx->mask, &ctx->d_in})
 		if (b->p)
 			cudaFree(b->p);
+	{
+		auto& B = ctx->batch;
+		for (DevBuf* b : {&B.doc_start, &B.items, &B.item_begin, &B.region_s, &B.region_b, &B.doc_cta, &B.sbase,
+						  &B.bbase, &B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.minbal, &B.maxbal,
+						  &B.flags, &B.cbase, &B.seg, &B.balanced, &B.well_formed, &B.max_depth, &B.cta_bcount,
+						  &B.bdoc, &B.dpos, &B.dsi, &B.ddepth, &B.dkey, &B.dkey_b, &B.order_b, &B.order})
+			if (b->p)
+				cudaFree(b->p);
+		if (B.bres)
+			cudaFree(B.bres);
+		if (B.helper)
+			pars_destroy(B.helper);
+	}
 	if (ctx->ctr) cudaFree(ctx->ctr);
 	if (ctx->rb) cudaFree(ctx->rb);
 	if (ctx->carry) cudaFree(ctx->carry);
@@ -1178,5 +1205,408 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 	void*	   fargs[] = {&r, &d_result};
 	CK(cudaLaunchKernel(noalloc_finish_kernel(), dim3(1), dim3(1), fargs, 0, st));
 	ctx->launches++;
+	return 0;
+}
+
+// ================================================================================
+// Batched documents
+// ================================================================================
+namespace pars {
+const void* batch_kernel(int which);
+}  // namespace pars
+
+namespace {
+
+constexpr uint32_t kMaxBatchDocs = 1u << 20;	 // the composite R6 key holds 20 document bits
+constexpr uint64_t kFallbackSlack = 1ull << 22;	 // output entries kept free for recomputed documents
+
+int ensure_batch_config(pars_ctx* ctx, int path, bool br) {
+	const int slot = path * 2 + (br ? 1 : 0);
+	if (ctx->batch.blocks[slot])
+		return 0;
+	const void* k	 = scan_ws_batch_kernel(path, br);
+	const int	smem = scan_ws_smem_bytes();
+	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	int per_sm = 0;
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, scan_ws_threads(), smem));
+	if (per_sm < 1)
+		return fail(ctx, PARS_ECUDA, "batch scan kernel does not fit on an SM");
+	ctx->batch.blocks[slot] = std::min(per_sm * ctx->num_sms, 1024);
+	return 0;
+}
+
+// LSD sort of `n_cap` int32 keys (count in res->n_brackets, minimum res->min_key) in
+// 8-bit digits; the stable order of indices lands in `order`.
+int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint32_t* order, uint64_t n_cap,
+			 DevResult* res, int passes, cudaStream_t st) {
+	const uint64_t ntiles_sort = (n_cap + sort_tile_keys() - 1) / sort_tile_keys() + 1;
+	if (int e = grow(ctx, ctx->lb, ntiles_sort * 256 * sizeof(uint64_t)))
+		return e;
+	if (int e = grow(ctx, ctx->digit_hist, 256 * 4))
+		return e;
+	if (int e = grow(ctx, ctx->sort_keys_a, n_cap * 4 + 16))
+		return e;
+	const int32_t*	kin	 = keys;
+	const uint32_t* iin	 = nullptr;
+	int32_t*		kbuf[2] = {static_cast<int32_t*>(ctx->sort_keys_a.p), kb};
+	uint32_t*		ibuf[2] = {order, ib};
+	int				out		= (passes % 2 == 1) ? 0 : 1;
+	for (int ps = 0; ps < passes; ++ps) {
+		CK(cudaMemsetAsync(ctx->digit_hist.p, 0, 256 * 4, st));
+		k_digit_hist<<<ctx->num_sms * 4, 256, 0, st>>>(kin, res, 8u * ps, static_cast<unsigned int*>(ctx->digit_hist.p));
+		CK(cudaGetLastError());
+		ctx->launches++;
+		SortPass sp {};
+		sp.keys_in	  = kin;
+		sp.idx_in	  = iin;
+		sp.keys_out	  = (ps + 1 < passes) ? kbuf[out] : nullptr;
+		sp.idx_out	  = ibuf[out];
+		sp.digit_hist = static_cast<const uint32_t*>(ctx->digit_hist.p);
+		sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
+		sp.ctr		  = ctx->ctr;
+		sp.res		  = res;
+		sp.key_hist	  = ctx->key_hist;
+		sp.cap		  = n_cap;
+		sp.shift	  = 8u * ps;
+		sp.epoch	  = next_epoch(ctx);
+		sp.first	  = 0;
+		void* a1[]	  = {&sp};
+		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4), dim3(256), a1, 0, st));
+		ctx->launches++;
+		kin = kbuf[out];
+		iin = ibuf[out];
+		out ^= 1;
+	}
+	return 0;
+}
+
+template<class T>
+int put(pars_ctx* ctx, DevBuf& b, const std::vector<T>& v, cudaStream_t st, const char* what) {
+	if (int e = grow_impl(ctx, b, v.size() * sizeof(T) + 16, what))
+		return e;
+	if (!v.empty())
+		CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+	return 0;
+}
+
+template<class T>
+int set1(pars_ctx* ctx, DevBuf& b, uint64_t i, T v, cudaStream_t st) {
+	CK(cudaMemcpyAsync(static_cast<T*>(b.p) + i, &v, sizeof(T), cudaMemcpyHostToDevice, st));
+	CK(cudaStreamSynchronize(st));	// `v` lives on this stack frame
+	return 0;
+}
+
+}  // namespace
+
+extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, const uint64_t* offsets,
+							   uint32_t ndocs, uint32_t flags, void* stream, pars_batch_result* out) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !out || !offsets)
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	if (ndocs > kMaxBatchDocs)
+		return fail(ctx, PARS_ERANGE, "more than 2^20 documents in one batch");
+	if (flags & (PARS_WANT_MASK | PARS_FORCE_GENERIC))
+		return fail(ctx, PARS_EINVAL, "batch scans produce no mask and run the fast paths");
+	for (uint32_t d = 0; d < ndocs; ++d)
+		if (offsets[d + 1] < offsets[d] || offsets[d + 1] - offsets[d] >= (1ull << 32))
+			return fail(ctx, PARS_ERANGE, "document offsets must not decrease; documents < 2^32 bytes");
+	if (offsets[0] != 0 || (offsets[ndocs] && !d_in))
+		return fail(ctx, PARS_EINVAL, "offsets must start at 0 and the input must be given");
+	cudaSetDevice(ctx->device);
+	cudaStream_t st	  = static_cast<cudaStream_t>(stream);
+	auto&		 B	  = ctx->batch;
+	const int	 path = pl->path;
+	const bool	 br	  = pl->host.has_brackets != 0;
+	const bool	 run_pairs = (flags & PARS_RUN_PAIRS) != 0;
+	std::memset(out, 0, sizeof *out);
+	out->ndocs = ndocs;
+
+	// ---- plan: documents to CTAs, largest first, each to the least loaded CTA --------
+	const uint64_t o	 = reinterpret_cast<uintptr_t>(d_in) & 127u;  // rows start on 128 bytes
+	const uint8_t* base	 = d_in - o;
+	const uint64_t total = o + offsets[ndocs];
+	const bool	   fast	 = use_ws(path);
+	int			   G	 = 1;
+	if (fast) {
+		if (int r = ensure_batch_config(ctx, path, br))
+			return r;
+		G = B.blocks[path * 2 + (br ? 1 : 0)];
+	}
+	std::vector<uint32_t> by_size(ndocs);
+	std::iota(by_size.begin(), by_size.end(), 0u);
+	std::stable_sort(by_size.begin(), by_size.end(), [&](uint32_t x, uint32_t y) {
+		return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
+	});
+	std::vector<std::vector<uint32_t>> cta_docs(G);
+	std::vector<uint64_t>			   load(G, 0);
+	{
+		using Slot = std::pair<uint64_t, int>;
+		std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> q;
+		for (int b = 0; b < G; ++b) q.push({0, b});
+		for (uint32_t d : by_size) {
+			Slot s = q.top();
+			q.pop();
+			const uint64_t sz = offsets[d + 1] - offsets[d];
+			cta_docs[s.second].push_back(d);
+			s.first += sz + 256;  // a document costs at least a tile's pipeline step
+			load[s.second] += sz;
+			q.push(s);
+		}
+	}
+	std::vector<uint64_t> doc_start(ndocs + 1), items;
+	std::vector<uint32_t> item_begin(G + 1), doc_cta(ndocs);
+	std::vector<uint64_t> region_s(G + 1), region_b(G + 1);
+	for (uint32_t d = 0; d <= ndocs; ++d) doc_start[d] = o + offsets[d];
+	items.reserve(ndocs + total / 32768 + 16);
+	for (int b = 0; b < G; ++b) {
+		item_begin[b] = static_cast<uint32_t>(items.size());
+		for (uint32_t d : cta_docs[b]) {
+			doc_cta[d] = static_cast<uint32_t>(b);
+			const uint64_t lo = doc_start[d], hi = doc_start[d + 1];
+			if (hi == lo)
+				continue;
+			const uint64_t nt = (hi - (lo & ~uint64_t(127)) + 32767) / 32768;
+			for (uint64_t j = 0; j < nt; ++j) items.push_back((static_cast<uint64_t>(d) << 32) | j);
+		}
+		region_s[b + 1] = region_s[b] + load[b] / 2 + 4096;
+		region_b[b + 1] = region_b[b] + (br ? load[b] / 4 + 4096 : 0);
+	}
+	item_begin[G] = static_cast<uint32_t>(items.size());
+	if (region_s[G] + kFallbackSlack >= (1ull << 32) || region_b[G] + kFallbackSlack >= (1ull << 32))
+		return fail(ctx, PARS_ERANGE, "batch outputs exceed 2^32 entries");
+
+	// ---- device buffers -------------------------------------------------------------
+	const uint64_t cap_s = region_s[G] + kFallbackSlack, cap_b = region_b[G] + kFallbackSlack;
+	const uint64_t nd	 = std::max<uint32_t>(ndocs, 1);
+	if (int e = put(ctx, B.doc_start, doc_start, st, "batch doc_start")) return e;
+	if (int e = put(ctx, B.items, items, st, "batch items")) return e;
+	if (int e = put(ctx, B.item_begin, item_begin, st, "batch item_begin")) return e;
+	if (int e = put(ctx, B.region_s, region_s, st, "batch region_s")) return e;
+	if (int e = put(ctx, B.region_b, region_b, st, "batch region_b")) return e;
+	if (int e = put(ctx, B.doc_cta, doc_cta, st, "batch doc_cta")) return e;
+	for (DevBuf* b : {&B.sbase, &B.bbase, &B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.flags, &B.cbase,
+					  &B.seg, &B.balanced, &B.well_formed, &B.max_depth})
+		if (int e = grow(ctx, *b, nd * 4 + 16))
+			return e;
+	for (DevBuf* b : {&B.minbal, &B.maxbal})
+		if (int e = grow(ctx, *b, nd * 8 + 16))
+			return e;
+	if (int e = grow(ctx, B.cta_bcount, static_cast<size_t>(G) * 4 + 16)) return e;
+	if (int e = grow(ctx, ctx->pos, cap_s * 4)) return e;
+	if ((flags & PARS_WANT_PAIRS) || run_pairs)
+		if (int e = grow(ctx, ctx->pair, cap_s * 4)) return e;
+	if (flags & PARS_WANT_CHARS)
+		if (int e = grow(ctx, ctx->chars, cap_s)) return e;
+	if (br) {
+		for (DevBuf* b : {&ctx->bpos, &ctx->bsi, &ctx->depth, &B.bdoc, &B.dpos, &B.dsi, &B.ddepth, &B.dkey, &B.dkey_b,
+						  &B.order_b, &B.order})
+			if (int e = grow(ctx, *b, cap_b * 4 + 16))
+				return e;
+	}
+	if (!B.bres)
+		CK(cudaMalloc(&B.bres, sizeof(DevResult)));
+	for (DevBuf* b : {&B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.flags, &B.cbase, &B.sbase, &B.bbase,
+					  &B.balanced, &B.well_formed, &B.max_depth})
+		CK(cudaMemsetAsync(b->p, 0, nd * 4, st));
+	CK(cudaMemsetAsync(B.minbal.p, 0, nd * 8, st));
+	CK(cudaMemsetAsync(B.maxbal.p, 0, nd * 8, st));
+	CK(cudaMemsetAsync(B.cta_bcount.p, 0, static_cast<size_t>(G) * 4, st));
+	CK(cudaMemsetAsync(B.bres, 0, sizeof(DevResult), st));
+	CK(cudaMemsetAsync(ctx->rb, 0, sizeof(ResBlock), st));
+
+	BatchDesc bd {};
+	bd.doc_start  = static_cast<const uint64_t*>(B.doc_start.p);
+	bd.items	  = static_cast<const uint64_t*>(B.items.p);
+	bd.item_begin = static_cast<const uint32_t*>(B.item_begin.p);
+	bd.region_s	  = static_cast<const uint64_t*>(B.region_s.p);
+	bd.region_b	  = static_cast<const uint64_t*>(B.region_b.p);
+	bd.sbase	  = static_cast<uint32_t*>(B.sbase.p);
+	bd.bbase	  = static_cast<uint32_t*>(B.bbase.p);
+	bd.nstruct	  = static_cast<uint32_t*>(B.nstruct.p);
+	bd.nopen	  = static_cast<uint32_t*>(B.nopen.p);
+	bd.nclose	  = static_cast<uint32_t*>(B.nclose.p);
+	bd.unclosed	  = static_cast<int32_t*>(B.unclosed.p);
+	bd.minbal	  = static_cast<unsigned long long*>(B.minbal.p);
+	bd.maxbal	  = static_cast<unsigned long long*>(B.maxbal.p);
+	bd.flags	  = static_cast<uint32_t*>(B.flags.p);
+	bd.cta_bcount = static_cast<uint32_t*>(B.cta_bcount.p);
+	bd.bdoc		  = static_cast<uint32_t*>(B.bdoc.p);
+
+	// ---- the persistent batch launch ------------------------------------------------------
+	std::vector<uint32_t> fall;	 // documents recomputed one by one
+	if (!fast) {
+		for (uint32_t d = 0; d < ndocs; ++d) fall.push_back(d);
+	} else if (!items.empty()) {
+		ScanArgs a {};
+		a.base	   = base;
+		a.o		   = 0;
+		a.n		   = total;
+		a.plan	   = pl->dev;
+		a.pos	   = static_cast<uint32_t*>(ctx->pos.p);
+		a.chars	   = static_cast<uint8_t*>(ctx->chars.p);
+		a.pair	   = static_cast<int32_t*>(ctx->pair.p);
+		a.bpos	   = static_cast<uint32_t*>(ctx->bpos.p);
+		a.bsi	   = static_cast<uint32_t*>(ctx->bsi.p);
+		a.depth	   = static_cast<int32_t*>(ctx->depth.p);
+		a.ctr	   = ctx->ctr;
+		a.res	   = ctx->res;
+		a.key_hist = ctx->key_hist;
+		a.epoch	   = next_epoch(ctx);
+		a.flags	   = flags & (PARS_WANT_PAIRS | PARS_WANT_CHARS);
+		if (run_pairs)
+			a.flags |= PARS_WANT_PAIRS;	 // R6 overwrites the brackets' entries
+		WsArgs		wa {a, total / 128, bd};
+		CUtensorMap map;
+		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+			return r;
+		void* wargs[] = {&wa, &map};
+		CK(cudaLaunchKernel(scan_ws_batch_kernel(path, br), dim3(G), dim3(scan_ws_threads()), wargs,
+							scan_ws_smem_bytes(), st));
+		ctx->launches++;
+		if (br) {
+			BatchR6 r6 {};
+			r6.doc_start   = bd.doc_start;
+			r6.doc_cta	   = static_cast<const uint32_t*>(B.doc_cta.p);
+			r6.region_b	   = bd.region_b;
+			r6.cta_bcount  = bd.cta_bcount;
+			r6.G		   = static_cast<uint32_t>(G);
+			r6.ndocs	   = ndocs;
+			r6.sbase	   = bd.sbase;
+			r6.bbase	   = bd.bbase;
+			r6.nopen	   = bd.nopen;
+			r6.nclose	   = bd.nclose;
+			r6.minbal	   = bd.minbal;
+			r6.maxbal	   = bd.maxbal;
+			r6.flags	   = bd.flags;
+			r6.cbase	   = static_cast<uint32_t*>(B.cbase.p);
+			r6.nbr		   = static_cast<uint32_t*>(B.nbr.p);
+			r6.seg		   = static_cast<uint32_t*>(B.seg.p);
+			r6.balanced	   = static_cast<int32_t*>(B.balanced.p);
+			r6.well_formed = static_cast<int32_t*>(B.well_formed.p);
+			r6.max_depth   = static_cast<int32_t*>(B.max_depth.p);
+			r6.bpos		   = static_cast<const uint32_t*>(ctx->bpos.p);
+			r6.bsi		   = static_cast<const uint32_t*>(ctx->bsi.p);
+			r6.bdoc		   = bd.bdoc;
+			r6.depth	   = static_cast<const int32_t*>(ctx->depth.p);
+			r6.dpos		   = static_cast<uint32_t*>(B.dpos.p);
+			r6.dsi		   = static_cast<uint32_t*>(B.dsi.p);
+			r6.ddepth	   = static_cast<int32_t*>(B.ddepth.p);
+			r6.dkey		   = static_cast<int32_t*>(B.dkey.p);
+			r6.order	   = static_cast<const uint32_t*>(B.order.p);
+			r6.pair		   = (flags & PARS_WANT_PAIRS) ? static_cast<int32_t*>(ctx->pair.p) : nullptr;
+			r6.in		   = base;
+			r6.plan		   = pl->dev;
+			r6.bres		   = B.bres;
+			void* ra[]	   = {&r6};
+			const int grid = ctx->num_sms * 4;
+			CK(cudaLaunchKernel(batch_kernel(0), dim3(grid), dim3(256), ra, 0, st));	 // compact
+			CK(cudaLaunchKernel(batch_kernel(1), dim3(grid), dim3(256), ra, 0, st));	 // docs
+			ctx->launches += 2;
+			if (run_pairs) {
+				if (int e = lsd_sort(ctx, static_cast<const int32_t*>(B.dkey.p), static_cast<int32_t*>(B.dkey_b.p),
+									 static_cast<uint32_t*>(B.order_b.p), static_cast<uint32_t*>(B.order.p), cap_b,
+									 B.bres, 4, st))
+					return e;
+				CK(cudaLaunchKernel(batch_kernel(2), dim3(grid), dim3(256), ra, 0, st));	 // segments
+				CK(cudaLaunchKernel(batch_kernel(3), dim3(grid), dim3(256), ra, 0, st));	 // pairs
+				ctx->launches += 2;
+			}
+		}
+		if (run_pairs) {
+			BatchR6 r6 {};
+			r6.ndocs	   = ndocs;
+			r6.nopen	   = bd.nopen;
+			r6.nclose	   = bd.nclose;
+			r6.minbal	   = bd.minbal;
+			r6.maxbal	   = bd.maxbal;
+			r6.flags	   = bd.flags;
+			r6.balanced	   = static_cast<int32_t*>(B.balanced.p);
+			r6.well_formed = static_cast<int32_t*>(B.well_formed.p);
+			r6.max_depth   = static_cast<int32_t*>(B.max_depth.p);
+			void* ra[]	   = {&r6};
+			CK(cudaLaunchKernel(batch_kernel(4), dim3(ctx->num_sms * 4), dim3(256), ra, 0, st));	 // flags
+			ctx->launches++;
+		}
+		// which documents need recomputing
+		B.h_flags.assign(nd, 0);
+		CK(cudaMemcpyAsync(B.h_flags.data(), B.flags.p, nd * 4, cudaMemcpyDeviceToHost, st));
+		DevResult hr {};
+		CK(cudaMemcpyAsync(&hr, ctx->res, sizeof hr, cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		if (hr.error) {
+			reset_after_error(ctx, st);
+			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+		}
+		for (uint32_t d = 0; d < ndocs; ++d)
+			if (B.h_flags[d] & (kBatchSpecFail | kBatchKeyRange | kBatchOverflow))
+				fall.push_back(d);
+	}
+
+	// ---- documents recomputed on their own, appended after the regions --------------------
+	if (!fall.empty()) {
+		if (!B.helper)
+			if (int e = pars_create(ctx->device, 0, &B.helper))
+				return fail(ctx, e, "could not create the helper context");
+		int hp = -1;
+		if (int e = pars_plan_load(B.helper, &pl->raw, sizeof pl->raw, &hp))
+			return fail(ctx, e, "helper plan load failed");
+		uint64_t s_cur = region_s[G], b_cur = 0;
+		if (br) {
+			uint32_t dense = 0;	// dense brackets in use
+			CK(cudaMemcpyAsync(&dense, &B.bres->n_brackets, 4, cudaMemcpyDeviceToHost, st));
+			CK(cudaStreamSynchronize(st));
+			b_cur = dense;
+		}
+		for (uint32_t d : fall) {
+			const uint64_t	   n = offsets[d + 1] - offsets[d];
+			pars_device_result r {};
+			if (int e = pars_scan_device(B.helper, hp, d_in + offsets[d], n, flags, stream, &r))
+				return fail(ctx, e, pars_last_error(B.helper));
+			if (s_cur + r.n_struct > cap_s || b_cur + r.n_brackets > cap_b)
+				return fail(ctx, PARS_ENOMEM, "recomputed documents exceed the batch's spare output room");
+			if (r.n_struct) {
+				CK(cudaMemcpyAsync(static_cast<uint32_t*>(ctx->pos.p) + s_cur, r.structural, r.n_struct * 4,
+								   cudaMemcpyDeviceToDevice, st));
+				if ((flags & PARS_WANT_PAIRS) && r.pair_pos)
+					CK(cudaMemcpyAsync(static_cast<int32_t*>(ctx->pair.p) + s_cur, r.pair_pos, r.n_struct * 4,
+									   cudaMemcpyDeviceToDevice, st));
+				if ((flags & PARS_WANT_CHARS) && r.chars)
+					CK(cudaMemcpyAsync(static_cast<uint8_t*>(ctx->chars.p) + s_cur, r.chars, r.n_struct,
+									   cudaMemcpyDeviceToDevice, st));
+			}
+			if (br && r.n_brackets) {
+				CK(cudaMemcpyAsync(static_cast<uint32_t*>(B.dpos.p) + b_cur, r.bracket_pos, r.n_brackets * 4,
+								   cudaMemcpyDeviceToDevice, st));
+				CK(cudaMemcpyAsync(static_cast<int32_t*>(B.ddepth.p) + b_cur, r.depth, r.n_brackets * 4,
+								   cudaMemcpyDeviceToDevice, st));
+			}
+			if (int e = set1<uint32_t>(ctx, B.sbase, d, static_cast<uint32_t>(s_cur), st)) return e;
+			if (int e = set1<uint32_t>(ctx, B.nstruct, d, static_cast<uint32_t>(r.n_struct), st)) return e;
+			if (int e = set1<uint32_t>(ctx, B.cbase, d, static_cast<uint32_t>(b_cur), st)) return e;
+			if (int e = set1<uint32_t>(ctx, B.nbr, d, static_cast<uint32_t>(r.n_brackets), st)) return e;
+			if (int e = set1<int32_t>(ctx, B.unclosed, d, r.unclosed_mode, st)) return e;
+			if (int e = set1<int32_t>(ctx, B.balanced, d, r.balanced, st)) return e;
+			if (int e = set1<int32_t>(ctx, B.well_formed, d, r.well_formed, st)) return e;
+			if (int e = set1<int32_t>(ctx, B.max_depth, d, r.max_depth, st)) return e;
+			s_cur += r.n_struct;
+			b_cur += r.n_brackets;
+		}
+	}
+	CK(cudaStreamSynchronize(st));
+	out->structural	   = static_cast<const uint32_t*>(ctx->pos.p);
+	out->chars		   = (flags & PARS_WANT_CHARS) ? static_cast<const uint8_t*>(ctx->chars.p) : nullptr;
+	out->pair_pos	   = (flags & PARS_WANT_PAIRS) ? static_cast<const int32_t*>(ctx->pair.p) : nullptr;
+	out->struct_off	   = static_cast<const uint32_t*>(B.sbase.p);
+	out->n_struct	   = static_cast<const uint32_t*>(B.nstruct.p);
+	out->bracket_pos   = br ? static_cast<const uint32_t*>(B.dpos.p) : nullptr;
+	out->depth		   = br ? static_cast<const int32_t*>(B.ddepth.p) : nullptr;
+	out->bracket_off   = static_cast<const uint32_t*>(B.cbase.p);
+	out->n_brackets	   = static_cast<const uint32_t*>(B.nbr.p);
+	out->unclosed_mode = static_cast<const int32_t*>(B.unclosed.p);
+	out->balanced	   = run_pairs ? static_cast<const int32_t*>(B.balanced.p) : nullptr;
+	out->well_formed   = run_pairs ? static_cast<const int32_t*>(B.well_formed.p) : nullptr;
+	out->max_depth	   = run_pairs ? static_cast<const int32_t*>(B.max_depth.p) : nullptr;
+	out->n_recomputed  = static_cast<uint32_t>(fall.size());
+	out->grid		   = static_cast<uint32_t>(G);
 	return 0;
 }

@@ -1,0 +1,156 @@
+// batch.cu — R6 and per-document results of a batch scan (pars_scan_batch).
+//
+// The batch scan (k_scan_ws<..., BATCH>) leaves each CTA's brackets in that CTA's
+// output region, in document order, with their document, byte offset, structural
+// index and depth key.  R6 per document (include/pars/model/nest.hpp:46-92) then
+// runs over all documents at once:
+//   k_batch_compact   regions -> one dense bracket array; composite key
+//                     document << 11 | (depth key + 1024)
+//   k_batch_docs      each document's dense bracket base
+//   4 x (k_digit_hist, k_sort_pass)   stable LSD sort of the composite keys
+//   k_batch_segstart  each document's segment start in (document, key) order
+//   k_batch_pair      adjacent pairing within each document's segment + type check
+//   k_batch_finalize  balanced / well_formed / max_depth per document
+// A stable sort by (document, key) is, within one document, the reference's stable
+// sort by key; pairing restarts at every segment start.  Keys outside [-1024, 1024)
+// were flagged by the scan: those documents are recomputed by the host.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace pars {
+
+namespace {
+
+constexpr int kMaxCtas = 1024;
+
+// Exclusive prefix of the per-CTA bracket counts, in shared memory (thread 0).
+__device__ void cta_prefix(const BatchR6& r, std::uint32_t* pre) {
+	if (threadIdx.x == 0) {
+		std::uint32_t s = 0;
+		for (std::uint32_t b = 0; b < r.G; ++b) {
+			pre[b] = s;
+			s += r.cta_bcount[b];
+		}
+		pre[r.G] = s;
+	}
+	__syncthreads();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_batch_compact(const BatchR6 r) {
+	__shared__ std::uint32_t pre[kMaxCtas + 1];
+	cta_prefix(r, pre);
+	const std::uint32_t total = pre[r.G];
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		r.bres->n_brackets = total;
+		r.bres->min_key	   = enc_min(0);
+		r.bres->max_key	   = enc_max(0x7FFFFFFF);
+	}
+	for (std::uint32_t i = blockIdx.x * 256u + threadIdx.x; i < total; i += gridDim.x * 256u) {
+		// the CTA whose region holds dense entry i
+		std::uint32_t lo = 0, hi = r.G;
+		while (hi - lo > 1) {
+			const std::uint32_t mid = (lo + hi) >> 1;
+			if (pre[mid] <= i)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		const std::uint64_t src = r.region_b[lo] + (i - pre[lo]);
+		const std::uint32_t d	= r.bdoc[src];
+		const std::int32_t	k	= r.depth[src];
+		r.dpos[i]				= r.bpos[src];
+		r.dsi[i]				= r.bsi[src];
+		r.ddepth[i]				= k;
+		const std::int32_t w	= k + kKeyWindow < 0 ? 0 : (k + kKeyWindow > 2 * kKeyWindow - 1 ? 2 * kKeyWindow - 1 : k + kKeyWindow);
+		r.dkey[i]				= static_cast<std::int32_t>((d << 11) | static_cast<std::uint32_t>(w));
+	}
+}
+
+__global__ void __launch_bounds__(256) k_batch_docs(const BatchR6 r) {
+	__shared__ std::uint32_t pre[kMaxCtas + 1];
+	cta_prefix(r, pre);
+	for (std::uint32_t d = blockIdx.x * 256u + threadIdx.x; d < r.ndocs; d += gridDim.x * 256u) {
+		const std::uint32_t b  = r.doc_cta[d];
+		const std::uint32_t nb = r.nopen[d] + r.nclose[d];
+		// a document without brackets (an empty one has no tiles and no base) points at 0
+		r.cbase[d] = nb ? pre[b] + static_cast<std::uint32_t>(r.bbase[d] - r.region_b[b]) : 0u;
+		r.nbr[d]   = nb;
+	}
+}
+
+// Where each document's segment starts in the sorted order (read from the keys, so
+// a document whose region overflowed cannot shift the others).
+__global__ void __launch_bounds__(256) k_batch_segstart(const BatchR6 r) {
+	const std::uint32_t total = static_cast<std::uint32_t>(r.bres->n_brackets);
+	for (std::uint32_t p = blockIdx.x * 256u + threadIdx.x; p < total; p += gridDim.x * 256u) {
+		const std::uint32_t d = static_cast<std::uint32_t>(r.dkey[r.order[p]]) >> 11;
+		if (p == 0 || (static_cast<std::uint32_t>(r.dkey[r.order[p - 1]]) >> 11) != d)
+			r.seg[d] = p;
+	}
+}
+
+__global__ void __launch_bounds__(256) k_batch_pair(const BatchR6 r) {
+	__shared__ std::uint8_t	 s_open[256], s_close[256];
+	__shared__ std::uint16_t s_first[256];
+	const int				 tid = threadIdx.x;
+	s_open[tid]				 = r.plan->is_open[tid];
+	s_close[tid]			 = r.plan->is_close[tid];
+	s_first[tid]			 = r.plan->first_close[tid];
+	__syncthreads();
+	const std::uint32_t total = static_cast<std::uint32_t>(r.bres->n_brackets);
+	for (std::uint32_t p = blockIdx.x * 256u + tid; p < total; p += gridDim.x * 256u) {
+		const std::uint32_t ia	  = r.order[p];
+		const std::uint32_t d	  = static_cast<std::uint32_t>(r.dkey[ia]) >> 11;
+		const std::uint32_t local = p - r.seg[d];
+		if (local & 1u)
+			continue;  // the second of a pair: handled with the first
+		if (r.flags[d] & (kBatchSpecFail | kBatchKeyRange | kBatchOverflow))
+			continue;  // recomputed by the host
+		const std::uint32_t sb = r.sbase[d];
+		if (p + 1 >= total || (static_cast<std::uint32_t>(r.dkey[r.order[p + 1]]) >> 11) != d) {
+			// odd count: the document's last entry has no partner
+			if (r.pair)
+				r.pair[sb + r.dsi[ia]] = -1;
+			continue;
+		}
+		const std::uint32_t ib = r.order[p + 1];
+		const std::uint64_t ds = r.doc_start[d];
+		const std::uint8_t	ca = r.in[ds + r.dpos[ia]], cb = r.in[ds + r.dpos[ib]];
+		const bool			ok = s_open[ca] && s_close[cb] && s_first[ca] == (0x100u | cb);
+		if (!ok)
+			atomicOr(&r.flags[d], kBatchMismatch);
+		if (r.pair) {
+			r.pair[sb + r.dsi[ia]] = ok ? static_cast<std::int32_t>(r.dsi[ib]) : -1;
+			r.pair[sb + r.dsi[ib]] = ok ? static_cast<std::int32_t>(r.dsi[ia]) : -1;
+		}
+	}
+}
+
+__global__ void __launch_bounds__(256) k_batch_finalize(const BatchR6 r) {
+	for (std::uint32_t d = blockIdx.x * 256u + threadIdx.x; d < r.ndocs; d += gridDim.x * 256u) {
+		const long long fin = static_cast<long long>(r.nopen[d]) - static_cast<long long>(r.nclose[d]);
+		const long long mnb = r.minbal[d] ? dec_min(r.minbal[d]) : 0;
+		const long long mxb = r.maxbal[d] ? dec_max(r.maxbal[d]) : 0;
+		const bool		bal = mnb >= 0 && fin == 0;
+		const std::uint32_t nb = r.nopen[d] + r.nclose[d];
+		r.balanced[d]	 = bal ? 1 : 0;
+		r.well_formed[d] = (bal && !(r.flags[d] & kBatchMismatch) && (nb % 2 == 0)) ? 1 : 0;
+		r.max_depth[d]	 = static_cast<std::int32_t>(mxb > 0 ? mxb : 0);
+	}
+}
+
+const void* batch_kernel(int which) {
+	switch (which) {
+		case 0: return reinterpret_cast<const void*>(&k_batch_compact);
+		case 1: return reinterpret_cast<const void*>(&k_batch_docs);
+		case 2: return reinterpret_cast<const void*>(&k_batch_segstart);
+		case 3: return reinterpret_cast<const void*>(&k_batch_pair);
+		case 4: return reinterpret_cast<const void*>(&k_batch_finalize);
+		default: return nullptr;
+	}
+}
+
+}  // namespace pars

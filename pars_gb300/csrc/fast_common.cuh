@@ -1,4 +1,5 @@
-// fast_common.cuh — pieces shared by the fast scan kernels (scan_fast.cu, scan_ws.cu).
+// fast_common.cuh — pieces of the warp-specialised scan kernel (scan_ws.cu): the
+// fast-path automaton algebra, hypothesis-packed counts and the R1 word classifier.
 #pragma once
 
 #include "scan_common.cuh"
@@ -6,34 +7,7 @@
 namespace pars {
 namespace scan_detail {
 
-constexpr std::uint32_t kDAgg  = 1u << 30;
-constexpr std::uint32_t kDIncl = 2u << 30;
-constexpr int			kRing  = 3;
 constexpr int			kLB	   = 5;	 // look-back words per lane of warp 0: G <= 32 * kLB
-
-// A look-back word is a uint4: three 32-bit payloads (x, y, z) and a tag w (flag,
-// epoch, element or state).  It is stored as three 64-bit words in planes [3][n],
-// each carrying the tag in its high half.  64 bits is the widest access the memory
-// model makes single-copy atomic; a 128-bit access can be observed half old, half
-// new.  A reader that sees the same tag in all three words has one publication;
-// differing tags read as "not yet published".
-__device__ __forceinline__ void st_desc(std::uint64_t* planes, std::uint64_t n, std::uint64_t i, const uint4& v) {
-	const std::uint64_t tag = static_cast<std::uint64_t>(v.w) << 32;
-	st_relaxed64(&planes[i], tag | v.x);
-	st_relaxed64(&planes[n + i], tag | v.y);
-	st_relaxed64(&planes[2 * n + i], tag | v.z);
-}
-
-__device__ __forceinline__ uint4 ld_desc(const std::uint64_t* planes, std::uint64_t n, std::uint64_t i) {
-	const std::uint64_t a = ld_relaxed64(&planes[i]);
-	const std::uint64_t b = ld_relaxed64(&planes[n + i]);
-	const std::uint64_t c = ld_relaxed64(&planes[2 * n + i]);
-	const std::uint32_t ta = static_cast<std::uint32_t>(a >> 32);
-	const std::uint32_t tb = static_cast<std::uint32_t>(b >> 32);
-	const std::uint32_t tc = static_cast<std::uint32_t>(c >> 32);
-	return make_uint4(static_cast<std::uint32_t>(a), static_cast<std::uint32_t>(b), static_cast<std::uint32_t>(c),
-					  (ta == tb && ta == tc) ? ta : 0u);
-}
 
 __device__ __forceinline__ std::uint32_t half16(std::uint32_t x, std::uint32_t h) {
 	return h ? (x >> 16) : (x & 0xFFFFu);

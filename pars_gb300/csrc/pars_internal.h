@@ -109,6 +109,73 @@ struct ResBlock {
 	unsigned int key_hist[2048];
 };
 
+// Batched documents (pars_scan_batch): one persistent launch scans many documents.
+// The host assigns whole documents to CTAs (largest first) and lists each CTA's
+// tiles; every CTA writes its documents' outputs into its own output regions.
+struct BatchDesc {
+	const std::uint64_t*  doc_start;   // [ndocs + 1] byte offsets into the batch input
+	const std::uint64_t*  items;	   // [nitems] document << 32 | tile within the document
+	const std::uint32_t*  item_begin;  // [G + 1] each CTA's range of items
+	const std::uint64_t*  region_s;	   // [G + 1] each CTA's structural output region
+	const std::uint64_t*  region_b;	   // [G + 1] each CTA's bracket output region
+	// per document
+	std::uint32_t*		  sbase;	   // first structural (output index)
+	std::uint32_t*		  bbase;	   // first bracket (output index)
+	std::uint32_t*		  nstruct;
+	std::uint32_t*		  nopen;
+	std::uint32_t*		  nclose;
+	std::int32_t*		  unclosed;
+	unsigned long long*	  minbal;	   // encoded extrema (zero = none)
+	unsigned long long*	  maxbal;
+	std::uint32_t*		  flags;	   // kBatch* bits
+	std::uint32_t*		  cta_bcount;  // [G] brackets written per CTA
+	std::uint32_t*		  bdoc;		   // [bracket output index] document of each bracket
+};
+
+// Arguments of the batch R6 kernels (batch.cu).
+struct BatchR6 {
+	const std::uint64_t* doc_start;	 // [ndocs + 1]
+	const std::uint32_t* doc_cta;	 // [ndocs] CTA that scanned each document
+	const std::uint64_t* region_b;	 // [G + 1]
+	const std::uint32_t* cta_bcount; // [G]
+	std::uint32_t		 G, ndocs;
+	const std::uint32_t* sbase;
+	const std::uint32_t* bbase;
+	const std::uint32_t* nopen;
+	const std::uint32_t* nclose;
+	const unsigned long long* minbal;
+	const unsigned long long* maxbal;
+	std::uint32_t*		 flags;
+	std::uint32_t*		 cbase;		 // [ndocs] first dense bracket of each document
+	std::uint32_t*		 nbr;		 // [ndocs] brackets of each document
+	std::uint32_t*		 seg;		 // [ndocs] segment start in (document, key) order
+	std::int32_t*		 balanced;
+	std::int32_t*		 well_formed;
+	std::int32_t*		 max_depth;
+	// the scan's bracket regions
+	const std::uint32_t* bpos;
+	const std::uint32_t* bsi;
+	const std::uint32_t* bdoc;
+	const std::int32_t*	 depth;
+	// dense brackets
+	std::uint32_t*		 dpos;
+	std::uint32_t*		 dsi;
+	std::int32_t*		 ddepth;
+	std::int32_t*		 dkey;
+	const std::uint32_t* order;		 // dense indices sorted by dkey (stable)
+	std::int32_t*		 pair;		 // structural-space pairs, or null
+	const std::uint8_t*	 in;		 // the batch input
+	const DevPlan*		 plan;
+	DevResult*			 bres;		 // total dense brackets and the key minimum (sort passes)
+};
+
+// Per-document flags of a batch scan.  Any of the first three means the document's
+// results came out incomplete and the host recomputes it on its own.
+constexpr std::uint32_t kBatchSpecFail = 1u;  // escape path: an escaped quote outside a string
+constexpr std::uint32_t kBatchKeyRange = 2u;  // a depth key outside [-1024, 1024)
+constexpr std::uint32_t kBatchOverflow = 4u;  // the CTA's output region was too small
+constexpr std::uint32_t kBatchMismatch = 8u;  // R6: a pair of mismatched bracket types
+
 // Fixed scratch of pars_scan_device_noalloc: [result block][counters][tile
 // descriptors], each part on a 256-byte boundary.  Sized for the largest input it
 // accepts with the largest descriptor (the general kernel's, one per 16 KiB tile).

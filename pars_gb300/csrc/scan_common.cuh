@@ -1,4 +1,4 @@
-// scan_common.cuh — helpers shared by the scan kernels (scan_fast.cu, scan.cu).
+// scan_common.cuh — helpers shared by the scan kernels (scan_ws.cu, scan.cu).
 #pragma once
 
 #include <cstdint>

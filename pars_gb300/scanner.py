@@ -192,6 +192,20 @@ class Scanner:
                                              ctypes.c_void_p(stream)),
               self.ctx.handle)
 
+    def scan_batch(self, d_ptr: int, offsets, stream: int = 0, want_pairs: bool = False,
+                   run_pairs: bool = True, want_chars: bool = False) -> "BatchView":
+        """pars_scan_batch over documents concatenated at device address `d_ptr`;
+        `offsets` (ndocs + 1 entries, from 0) delimit them."""
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        flags = ((PARS_WANT_PAIRS if want_pairs else 0) | (PARS_RUN_PAIRS if run_pairs else 0)
+                 | (PARS_WANT_CHARS if want_chars else 0))
+        r = _lib.BatchResult()
+        check(lib().pars_scan_batch(self.ctx.handle, self.plan_id, ctypes.c_void_p(d_ptr),
+                                    off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                    off.size - 1, flags, ctypes.c_void_p(stream), ctypes.byref(r)),
+              self.ctx.handle)
+        return BatchView(r)
+
     def scan_tensor(self, t, **kw) -> DeviceResult:
         """scan_device on a contiguous uint8 CUDA tensor."""
         import torch
@@ -242,3 +256,58 @@ class Scanner:
         check(lib().pars_chunk_finish(self.ctx.handle, self.plan_id, ctypes.byref(carry), flags,
                                       ctypes.c_void_p(stream), ctypes.byref(r)), self.ctx.handle)
         return DeviceResult(r, int(carry.byte_base))
+
+
+class BatchView:
+    """Host view of a pars_batch_result: copies the per-document arrays once and
+    serves each document's outputs as numpy arrays."""
+
+    def __init__(self, r):
+        self.raw = r
+        n = r.ndocs
+        self.ndocs = n
+        self.n_recomputed = r.n_recomputed
+        self.grid = r.grid
+
+        def vec(ptr, dtype, count):
+            if not ptr or count == 0:
+                return None
+            out = np.empty(count, dtype)
+            _copy_d2h(out, ptr)
+            return out
+
+        self.struct_off = vec(r.struct_off, np.uint32, n)
+        self.n_struct = vec(r.n_struct, np.uint32, n)
+        self.bracket_off = vec(r.bracket_off, np.uint32, n)
+        self.n_brackets = vec(r.n_brackets, np.uint32, n)
+        self.unclosed_mode = vec(r.unclosed_mode, np.int32, n)
+        self.balanced = vec(r.balanced, np.int32, n)
+        self.well_formed = vec(r.well_formed, np.int32, n)
+        self.max_depth = vec(r.max_depth, np.int32, n)
+        se = int((self.struct_off.astype(np.int64) + self.n_struct).max()) if n else 0
+        be = int((self.bracket_off.astype(np.int64) + self.n_brackets).max()) if n else 0
+        self.structural = vec(r.structural, np.uint32, se)
+        self.pair_pos = vec(r.pair_pos, np.int32, se)
+        self.chars = vec(r.chars, np.uint8, se)
+        self.bracket_pos = vec(r.bracket_pos, np.uint32, be)
+        self.depth = vec(r.depth, np.int32, be)
+
+    def doc(self, d: int) -> dict:
+        s0, ns = int(self.struct_off[d]), int(self.n_struct[d])
+        b0, nb = int(self.bracket_off[d]), int(self.n_brackets[d])
+        cut = lambda a, o, c: (a[o:o + c] if a is not None else None)  # noqa: E731
+        return {"pos": cut(self.structural, s0, ns), "pair": cut(self.pair_pos, s0, ns),
+                "chars": cut(self.chars, s0, ns), "bpos": cut(self.bracket_pos, b0, nb),
+                "depth": cut(self.depth, b0, nb), "unclosed_mode": int(self.unclosed_mode[d]),
+                "balanced": None if self.balanced is None else int(self.balanced[d]),
+                "well_formed": None if self.well_formed is None else int(self.well_formed[d]),
+                "max_depth": None if self.max_depth is None else int(self.max_depth[d])}
+
+
+def _copy_d2h(out: np.ndarray, ptr: int) -> None:
+    """Copies device memory at `ptr` into `out`."""
+    import torch
+    typestr = {np.dtype(np.uint32): "<u4", np.dtype(np.int32): "<i4", np.dtype(np.uint8): "|u1"}[out.dtype]
+    tdt = {np.dtype(np.uint32): torch.int32, np.dtype(np.int32): torch.int32, np.dtype(np.uint8): torch.uint8}[out.dtype]
+    t = _view(ptr, out.size, typestr, tdt)
+    out[:] = t.cpu().numpy().view(out.dtype)

@@ -1,0 +1,95 @@
+"""pars_scan_batch: every document of a batch must come out exactly as
+pars_scan_device makes it on that document alone (offsets, pairs, bracket offsets,
+depth keys, unclosed_mode, balanced / well_formed / max_depth)."""
+import numpy as np
+import pytest
+
+from conftest import plan_bytes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from pars_gb300 import Context, Scanner, synth  # noqa: E402
+
+
+def lognormal_docs(seed, n, gen, median=2048, sigma=1.5, lo=64, hi=1 << 20):
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.exp(rng.normal(np.log(median), sigma, n)), lo, hi).astype(np.int64)
+    return [gen(seed * 1000 + i, int(s)) for i, s in enumerate(sizes)]
+
+
+def concat(docs):
+    offs = np.zeros(len(docs) + 1, np.uint64)
+    offs[1:] = np.cumsum([d.size for d in docs])
+    data = np.concatenate(docs) if docs else np.zeros(0, np.uint8)
+    return data, offs
+
+
+def check_batch(sc, docs, offset=0, want_pairs=True):
+    data, offs = concat(docs)
+    buf = torch.zeros(data.size + offset + 64, dtype=torch.uint8, device="cuda")
+    if data.size:
+        buf[offset:offset + data.size] = torch.from_numpy(data).cuda()
+    bv = sc.scan_batch(buf.data_ptr() + offset, offs, want_pairs=want_pairs)
+    torch.cuda.synchronize()
+    for d, doc in enumerate(docs):
+        got = bv.doc(d)
+        t = torch.from_numpy(doc).cuda() if doc.size else torch.zeros(1, dtype=torch.uint8, device="cuda")
+        r = sc.scan_device(t.data_ptr(), doc.size, want_pairs=want_pairs)
+        torch.cuda.synchronize()
+        e = r.to_numpy()
+        name = f"doc {d} ({doc.size} B)"
+        assert np.array_equal(got["pos"], e["pos"]), name
+        if want_pairs:
+            assert np.array_equal(got["pair"], e["pair"]), name
+        if got["bpos"] is not None:
+            assert np.array_equal(got["bpos"], e["bpos"]), name
+            assert np.array_equal(got["depth"], e["depth"]), name
+        assert got["unclosed_mode"] == r.unclosed_mode, name
+        assert (got["balanced"], got["well_formed"], got["max_depth"]) == \
+            (int(r.balanced), int(r.well_formed), r.max_depth), name
+    return bv
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return Context(0)
+
+
+def test_batch_json_lognormal(ctx):
+    sc = Scanner(plan_bytes("json"), ctx=ctx)
+    docs = lognormal_docs(3, 1500, synth.json_doc)
+    bv = check_batch(sc, docs)
+    assert bv.n_recomputed == 0
+
+
+def test_batch_csv_lognormal_unaligned(ctx):
+    sc = Scanner(plan_bytes("csv"), ctx=ctx)
+    docs = lognormal_docs(5, 800, synth.csv_doc)
+    check_batch(sc, docs, offset=3)
+
+
+def test_batch_edge_documents(ctx):
+    sc = Scanner(plan_bytes("json"), ctx=ctx)
+    docs = [np.frombuffer(x, np.uint8).copy() for x in (
+        b"", b"[", b"]", b"{}", b'"abc', b'"a\\"b" : [1,2]', b'[1, \\"x", 2]',  # escaped quote outside: recomputed
+        b"[" * 1500 + b"]" * 1500,                      # deeper than the key window: recomputed
+        b"]" * 1100,                                    # keys below -1024: recomputed
+        b"[1, {2]}", b"[[[]]", b'{"k": "v\\\\"}', b"",
+    )]
+    docs += lognormal_docs(7, 200, synth.json_doc, median=300, sigma=1.0)
+    bv = check_batch(sc, docs)
+    assert bv.n_recomputed >= 3
+
+
+def test_batch_generic_plan(ctx):
+    sc = Scanner(plan_bytes("toml"), ctx=ctx)
+    docs = lognormal_docs(9, 60, synth.csv_doc, median=1000, sigma=1.0)
+    bv = check_batch(sc, docs)
+    assert bv.n_recomputed == len(docs)
+
+
+def test_batch_empty(ctx):
+    sc = Scanner(plan_bytes("json"), ctx=ctx)
+    bv = sc.scan_batch(0, np.zeros(1, np.uint64))
+    assert bv.ndocs == 0
