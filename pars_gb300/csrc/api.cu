@@ -1332,25 +1332,45 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			return r;
 		G = B.blocks[path * 2 + (br ? 1 : 0)];
 	}
-	std::vector<uint32_t> by_size(ndocs);
-	std::iota(by_size.begin(), by_size.end(), 0u);
-	std::stable_sort(by_size.begin(), by_size.end(), [&](uint32_t x, uint32_t y) {
-		return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
-	});
+	// Large documents (over a quarter of a CTA's share) go largest first to the least
+	// loaded CTA; the many small ones then fill the CTAs up to the mean load in one
+	// pass.  The plan is within one small document of LPT's balance.
 	std::vector<std::vector<uint32_t>> cta_docs(G);
 	std::vector<uint64_t>			   load(G, 0);
 	{
+		const uint64_t share = offsets[ndocs] / static_cast<uint64_t>(G) + 1;
+		std::vector<uint32_t> big;
+		for (uint32_t d = 0; d < ndocs; ++d)
+			if (offsets[d + 1] - offsets[d] > share / 4)
+				big.push_back(d);
+		std::sort(big.begin(), big.end(), [&](uint32_t x, uint32_t y) {
+			const uint64_t sx = offsets[x + 1] - offsets[x], sy = offsets[y + 1] - offsets[y];
+			return sx != sy ? sx > sy : x < y;
+		});
 		using Slot = std::pair<uint64_t, int>;
 		std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> q;
 		for (int b = 0; b < G; ++b) q.push({0, b});
-		for (uint32_t d : by_size) {
-			Slot s = q.top();
+		for (uint32_t d : big) {
+			Slot sl = q.top();
 			q.pop();
+			cta_docs[sl.second].push_back(d);
+			sl.first += offsets[d + 1] - offsets[d];
+			load[sl.second] = sl.first;
+			q.push(sl);
+		}
+		// CTAs by load, lightest first; each takes small documents up to the mean
+		std::vector<int> by_load(G);
+		std::iota(by_load.begin(), by_load.end(), 0);
+		std::sort(by_load.begin(), by_load.end(), [&](int x, int y) { return load[x] < load[y]; });
+		const uint64_t mean = (offsets[ndocs] + static_cast<uint64_t>(G) - 1) / static_cast<uint64_t>(G);
+		int			   ci	= 0;
+		for (uint32_t d = 0; d < ndocs; ++d) {
 			const uint64_t sz = offsets[d + 1] - offsets[d];
-			cta_docs[s.second].push_back(d);
-			s.first += sz + 256;  // a document costs at least a tile's pipeline step
-			load[s.second] += sz;
-			q.push(s);
+			if (sz > share / 4)
+				continue;
+			while (ci + 1 < G && load[by_load[ci]] + sz / 2 > mean) ++ci;
+			cta_docs[by_load[ci]].push_back(d);
+			load[by_load[ci]] += sz;
 		}
 	}
 	std::vector<uint64_t> doc_start(ndocs + 1), items;

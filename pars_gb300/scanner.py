@@ -193,9 +193,10 @@ class Scanner:
               self.ctx.handle)
 
     def scan_batch(self, d_ptr: int, offsets, stream: int = 0, want_pairs: bool = False,
-                   run_pairs: bool = True, want_chars: bool = False) -> "BatchView":
+                   run_pairs: bool = True, want_chars: bool = False, host_view: bool = True):
         """pars_scan_batch over documents concatenated at device address `d_ptr`;
-        `offsets` (ndocs + 1 entries, from 0) delimit them."""
+        `offsets` (ndocs + 1 entries, from 0) delimit them.  Returns a BatchView (host
+        copies), or with host_view=False the raw pars_batch_result (device pointers)."""
         off = np.ascontiguousarray(offsets, dtype=np.uint64)
         flags = ((PARS_WANT_PAIRS if want_pairs else 0) | (PARS_RUN_PAIRS if run_pairs else 0)
                  | (PARS_WANT_CHARS if want_chars else 0))
@@ -204,7 +205,7 @@ class Scanner:
                                     off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                                     off.size - 1, flags, ctypes.c_void_p(stream), ctypes.byref(r)),
               self.ctx.handle)
-        return BatchView(r)
+        return BatchView(r) if host_view else r
 
     def scan_tensor(self, t, **kw) -> DeviceResult:
         """scan_device on a contiguous uint8 CUDA tensor."""
