@@ -274,6 +274,81 @@ def batched_leg(args, stream, barrier, world, peak, ndocs=100_000, sample=2000):
             "timing": "wall clock of the blocking call, host planning and result flags included"}
 
 
+def serving_leg(args, seconds=0.6, loads=(0.1, 0.5, 0.9, 1.2)):
+    """Serving: Poisson arrivals of mixed requests (70% JSON, 30% CSV, sizes
+    log-uniform 256 B - 64 MiB, drawn from a seeded pool of pinned documents),
+    memory-admitted into an 8 GiB device arena.  Capacity is the throughput with all
+    requests queued at once; offered load then sweeps fractions of it.  The plain
+    per-request path (one launch per request) runs at the same offered rates."""
+    import torch
+    from pars_gb300 import synth
+    from pars_gb300.server import Server
+    rng = np.random.default_rng(SEED)
+    pool = []
+    for i in range(40):
+        g = "json" if i % 10 < 7 else "csv"
+        size = int(np.exp(rng.uniform(np.log(256), np.log(64 << 20))))
+        d = synth.json_doc(SEED + i, size) if g == "json" else synth.csv_doc(SEED + i, size)
+        pool.append((g, torch.from_numpy(d).pin_memory()))
+
+    def run(srv, plans, rate, n_req, seed):
+        r = np.random.default_rng(seed)
+        picks = r.integers(0, len(pool), n_req)
+        gaps = r.exponential(1.0 / rate, n_req) if rate else np.zeros(n_req)
+        tickets, nbytes = [], 0
+        t0 = time.perf_counter()
+        due = t0
+        for i in range(n_req):
+            due += gaps[i]
+            while True:
+                left = due - time.perf_counter()
+                if left <= 0:
+                    break
+                if left > 2e-4:
+                    time.sleep(left - 1e-4)
+            g, t = pool[picks[i]]
+            tickets.append(srv.submit(plans[g], t.data_ptr(), t.numel()))
+            nbytes += t.numel()
+        lat, folded, first, last = [], 0, None, 0
+        for tk in tickets:
+            res = srv.wait(tk, copy=False)
+            lat.append(res["latency_ns"] / 1e6)
+            folded += res["batch_docs"]
+            first = res["submit_ns"] if first is None else min(first, res["submit_ns"])
+            last = max(last, res["done_ns"])
+        wall = (last - first) / 1e9	 # the server's clock: first submission to last completion
+        lat = np.array(lat)
+        return {"requests": n_req, "GBps": round(nbytes / wall / 1e9, 3),
+                "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "p999_ms": round(float(np.percentile(lat, 99.9)), 3),
+                "mean_docs_per_launch": round(folded / max(n_req, 1), 2)}, nbytes, wall
+
+    out = {"workload": "serving_mixed_json70_csv30_logu_256B_64MiB", "arena_bytes": 8 << 30}
+    paths = {"batched": Server(arena_bytes=8 << 30, workers=2, max_batch_docs=4096),
+             "plain": Server(arena_bytes=8 << 30, workers=1, max_batch_docs=1)}
+    plans = {k: {g: srv.load_plan(plan(g)) for g in ("json", "csv")} for k, srv in paths.items()}
+    run(paths["batched"], plans["batched"], None, 40, 1)	 # warm-up
+    run(paths["plain"], plans["plain"], None, 40, 1)
+    cap, nb, wall = run(paths["batched"], plans["batched"], None, 400, 2)
+    cap_rps = 400 / wall
+    out["capacity"] = {"GBps": cap["GBps"], "requests_per_s": round(cap_rps, 1)}
+    for k in paths:
+        out[k] = []
+    for f in loads:
+        rate = f * cap_rps
+        n_req = max(40, int(rate * seconds))
+        for k, srv in paths.items():
+            res, _, _ = run(srv, plans[k], rate, n_req, int(f * 1000) + 7)
+            res["offered_load"] = f
+            res["offered_requests_per_s"] = round(rate, 1)
+            out[k].append(res)
+    for srv in paths.values():
+        srv.close()
+    out["timing"] = "latency = completion - submission (server steady clock), results in host memory"
+    return out
+
+
 def ctypes_float():
     import ctypes
     return ctypes.c_float()
@@ -288,6 +363,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -380,6 +456,9 @@ def main():
     batched = None
     if not args.no_batched:
         batched = batched_leg(args, stream, barrier, world, peak)
+    serving = None
+    if not args.no_serving and rank == 0:
+        serving = serving_leg(args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -406,6 +485,7 @@ def main():
             "cpu_baseline": cpu,
             "secondary": secondary,
             "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

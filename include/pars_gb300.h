@@ -167,16 +167,18 @@ int pars_chunk_finish(pars_ctx* ctx, int plan_id, const pars_chunk_carry* carry,
  * whole documents (largest first), the scan state resets at every document start,
  * and R6 pairs every document's brackets in one sort keyed by (document, depth).
  * Each document's results are exactly those of pars_scan_device on it alone.
- * Documents the fast kernel cannot finish on its own (an escaped quote outside a
- * string, depth keys beyond +-1024, an output region too small) and plans without a
- * fast path are recomputed one by one inside the call (n_recomputed counts them).
+ * Documents over 8 MiB would hold one CTA too long: they run one at a time on the
+ * whole grid (the single-document kernel).  Documents the batch kernel cannot
+ * finish (an escaped quote outside a string, depth keys beyond +-1024, an output
+ * region too small) and plans without a fast path are rescanned one by one inside
+ * the call (n_recomputed counts them).
  * Blocks until the results are ready; pointers stay valid until the next batch
  * call on the context. */
 typedef struct pars_batch_result {
   uint32_t ndocs;
   uint32_t grid;                 /* CTAs of the persistent launch                      */
-  uint32_t n_recomputed;
-  uint32_t reserved;
+  uint32_t n_recomputed;          /* documents the batch kernel flagged, then rescanned */
+  uint32_t n_whole_grid;          /* documents over 8 MiB: scanned on the whole grid   */
   /* document d: structural[struct_off[d] .. struct_off[d] + n_struct[d]), byte
    * offsets relative to the document's start; pair_pos (PARS_WANT_PAIRS) and chars
    * (PARS_WANT_CHARS) use the same indexing, pair_pos in the document's own
@@ -202,6 +204,48 @@ typedef struct pars_batch_result {
  * At most 2^20 documents, each < 2^32 bytes.  PARS_WANT_MASK is not supported. */
 int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, const uint64_t* offsets,
                     uint32_t ndocs, uint32_t flags, void* stream, pars_batch_result* out);
+
+/* ---- serving: continuous batching --------------------------------------- */
+/* No counterpart in the reference.  A request server: parse requests of any loaded
+ * plan and size are submitted from any thread; `workers` host threads each own a
+ * context, a stream and an arena_bytes / workers slice of a device input arena.
+ * An idle worker admits the oldest pending request's plan and every pending
+ * request of that plan that fits its free slice (up to max_batch_docs), uploads
+ * them and scans them in one pars_scan_batch launch; requests that arrive while
+ * a launch runs are admitted by the next free worker, so their work overlaps on the
+ * device.  max_batch_docs = 1 runs the plain path, one pars_scan_device launch per
+ * request.  Each result equals pars_scan_device on the request alone. */
+typedef struct pars_server pars_server;
+
+typedef struct pars_server_config {
+  int device;
+  uint32_t workers;              /* launches in flight (0: 2)                         */
+  uint64_t arena_bytes;          /* device memory for admitted inputs                 */
+  uint32_t max_batch_docs;       /* requests folded into one launch (1: plain path)   */
+  uint32_t reserved;
+} pars_server_config;
+
+typedef struct pars_server_result {
+  const uint32_t* structural;    /* host memory, valid until pars_server_release       */
+  const int32_t* pair_pos;       /* with PARS_WANT_PAIRS, else NULL                    */
+  uint64_t n_struct;
+  int32_t balanced, well_formed, max_depth, unclosed_mode;
+  int32_t status;                /* 0 or a PARS_E* code for this request               */
+  uint32_t batch_docs;           /* requests folded into the launch that carried it    */
+  uint64_t submit_ns, start_ns, done_ns;  /* steady clock: queued, launched, finished */
+} pars_server_result;
+
+int pars_server_create(const pars_server_config* cfg, pars_server** out);
+int pars_server_destroy(pars_server* srv);
+int pars_server_plan_load(pars_server* srv, const void* scan_plan, size_t len, int* plan_id);
+/* `data` (host memory; pinned uploads fastest) must stay readable until the request
+ * is reported done.  flags: PARS_WANT_PAIRS (R6 always runs). */
+int pars_server_submit(pars_server* srv, int plan_id, const uint8_t* data, uint64_t n,
+                       uint32_t flags, uint64_t* ticket);
+/* 0 and the result when done, PARS_EAGAIN while pending. */
+int pars_server_poll(pars_server* srv, uint64_t ticket, pars_server_result* out);
+int pars_server_wait(pars_server* srv, uint64_t ticket, pars_server_result* out);
+int pars_server_release(pars_server* srv, uint64_t ticket);
 
 /* ---- scan without allocation ---------------------------------------------- */
 /* No counterpart in the reference (whose scanner always owns a DeviceCache that

@@ -69,7 +69,7 @@ PARS_NOALLOC_MAX_BYTES = 134217728
 class BatchResult(ctypes.Structure):
     """pars_batch_result: device pointers, per-document arrays of `ndocs` entries."""
     _fields_ = [("ndocs", ctypes.c_uint32), ("grid", ctypes.c_uint32),
-                ("n_recomputed", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("n_recomputed", ctypes.c_uint32), ("n_whole_grid", ctypes.c_uint32),
                 ("structural", ctypes.c_void_p), ("pair_pos", ctypes.c_void_p),
                 ("chars", ctypes.c_void_p), ("struct_off", ctypes.c_void_p),
                 ("n_struct", ctypes.c_void_p), ("bracket_pos", ctypes.c_void_p),
@@ -77,6 +77,21 @@ class BatchResult(ctypes.Structure):
                 ("n_brackets", ctypes.c_void_p), ("unclosed_mode", ctypes.c_void_p),
                 ("balanced", ctypes.c_void_p), ("well_formed", ctypes.c_void_p),
                 ("max_depth", ctypes.c_void_p)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("workers", ctypes.c_uint32),
+                ("arena_bytes", ctypes.c_uint64), ("max_batch_docs", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("structural", ctypes.c_void_p), ("pair_pos", ctypes.c_void_p),
+                ("n_struct", ctypes.c_uint64), ("balanced", ctypes.c_int32),
+                ("well_formed", ctypes.c_int32), ("max_depth", ctypes.c_int32),
+                ("unclosed_mode", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("batch_docs", ctypes.c_uint32), ("submit_ns", ctypes.c_uint64),
+                ("start_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64)]
 
 
 # Every function the header declares, with its ctypes signature.
@@ -110,6 +125,15 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
                                        ctypes.c_uint32, ctypes.c_void_p,
                                        ctypes.POINTER(BatchResult)]),
+    "pars_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "pars_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pars_server_plan_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                             ctypes.POINTER(ctypes.c_int)]),
+    "pars_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                          ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
+    "pars_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ServerResult)]),
+    "pars_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ServerResult)]),
+    "pars_server_release": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "pars_scan_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.c_void_p, ctypes.c_void_p]),

@@ -1219,6 +1219,7 @@ namespace {
 
 constexpr uint32_t kMaxBatchDocs = 1u << 20;	 // the composite R6 key holds 20 document bits
 constexpr uint64_t kFallbackSlack = 1ull << 22;	 // output entries kept free for recomputed documents
+constexpr uint64_t kSoloBytes	  = 8ull << 20;	 // larger documents run on the whole grid, one at a time
 
 int ensure_batch_config(pars_ctx* ctx, int path, bool br) {
 	const int slot = path * 2 + (br ? 1 : 0);
@@ -1289,12 +1290,6 @@ int put(pars_ctx* ctx, DevBuf& b, const std::vector<T>& v, cudaStream_t st, cons
 	return 0;
 }
 
-template<class T>
-int set1(pars_ctx* ctx, DevBuf& b, uint64_t i, T v, cudaStream_t st) {
-	CK(cudaMemcpyAsync(static_cast<T*>(b.p) + i, &v, sizeof(T), cudaMemcpyHostToDevice, st));
-	CK(cudaStreamSynchronize(st));	// `v` lives on this stack frame
-	return 0;
-}
 
 }  // namespace
 
@@ -1335,14 +1330,30 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	// Large documents (over a quarter of a CTA's share) go largest first to the least
 	// loaded CTA; the many small ones then fill the CTAs up to the mean load in one
 	// pass.  The plan is within one small document of LPT's balance.
+	// Documents over kSoloBytes would hold one CTA for too long: they run on the whole
+	// grid with the single-document kernel instead (after the batch launch).
 	std::vector<std::vector<uint32_t>> cta_docs(G);
 	std::vector<uint64_t>			   load(G, 0);
+	std::vector<uint32_t>			   solo;
+	uint64_t						   solo_bytes = 0, batch_bytes = 0;
+	for (uint32_t d = 0; d < ndocs; ++d) {
+		const uint64_t sz = offsets[d + 1] - offsets[d];
+		if (fast && sz > kSoloBytes) {
+			solo.push_back(d);
+			solo_bytes += sz;
+		} else {
+			batch_bytes += sz;
+		}
+	}
+	auto is_solo = [&](uint64_t sz) { return fast && sz > kSoloBytes; };
 	{
-		const uint64_t share = offsets[ndocs] / static_cast<uint64_t>(G) + 1;
+		const uint64_t share = batch_bytes / static_cast<uint64_t>(G) + 1;
 		std::vector<uint32_t> big;
-		for (uint32_t d = 0; d < ndocs; ++d)
-			if (offsets[d + 1] - offsets[d] > share / 4)
+		for (uint32_t d = 0; d < ndocs; ++d) {
+			const uint64_t sz = offsets[d + 1] - offsets[d];
+			if (sz > share / 4 && !is_solo(sz))
 				big.push_back(d);
+		}
 		std::sort(big.begin(), big.end(), [&](uint32_t x, uint32_t y) {
 			const uint64_t sx = offsets[x + 1] - offsets[x], sy = offsets[y + 1] - offsets[y];
 			return sx != sy ? sx > sy : x < y;
@@ -1362,11 +1373,11 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		std::vector<int> by_load(G);
 		std::iota(by_load.begin(), by_load.end(), 0);
 		std::sort(by_load.begin(), by_load.end(), [&](int x, int y) { return load[x] < load[y]; });
-		const uint64_t mean = (offsets[ndocs] + static_cast<uint64_t>(G) - 1) / static_cast<uint64_t>(G);
+		const uint64_t mean = (batch_bytes + static_cast<uint64_t>(G) - 1) / static_cast<uint64_t>(G);
 		int			   ci	= 0;
 		for (uint32_t d = 0; d < ndocs; ++d) {
 			const uint64_t sz = offsets[d + 1] - offsets[d];
-			if (sz > share / 4)
+			if (sz > share / 4 || is_solo(sz))
 				continue;
 			while (ci + 1 < G && load[by_load[ci]] + sz / 2 > mean) ++ci;
 			cta_docs[by_load[ci]].push_back(d);
@@ -1392,11 +1403,14 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		region_b[b + 1] = region_b[b] + (br ? load[b] / 4 + 4096 : 0);
 	}
 	item_begin[G] = static_cast<uint32_t>(items.size());
-	if (region_s[G] + kFallbackSlack >= (1ull << 32) || region_b[G] + kFallbackSlack >= (1ull << 32))
+	// room after the regions: whole-grid documents (bounded by their bytes) and slack
+	// for documents the batch kernel flags
+	const uint64_t extra = solo_bytes + kFallbackSlack;
+	if (region_s[G] + extra >= (1ull << 32) || region_b[G] + extra >= (1ull << 32))
 		return fail(ctx, PARS_ERANGE, "batch outputs exceed 2^32 entries");
 
 	// ---- device buffers -------------------------------------------------------------
-	const uint64_t cap_s = region_s[G] + kFallbackSlack, cap_b = region_b[G] + kFallbackSlack;
+	const uint64_t cap_s = region_s[G] + extra, cap_b = region_b[G] + (br ? extra : kFallbackSlack);
 	const uint64_t nd	 = std::max<uint32_t>(ndocs, 1);
 	if (int e = put(ctx, B.doc_start, doc_start, st, "batch doc_start")) return e;
 	if (int e = put(ctx, B.items, items, st, "batch items")) return e;
@@ -1453,7 +1467,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	bd.bdoc		  = static_cast<uint32_t*>(B.bdoc.p);
 
 	// ---- the persistent batch launch ------------------------------------------------------
-	std::vector<uint32_t> fall;	 // documents recomputed one by one
+	std::vector<uint32_t> fall = solo;	// documents scanned one by one
 	if (!fast) {
 		for (uint32_t d = 0; d < ndocs; ++d) fall.push_back(d);
 	} else if (!items.empty()) {
@@ -1558,7 +1572,8 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
 		}
 		for (uint32_t d = 0; d < ndocs; ++d)
-			if (B.h_flags[d] & (kBatchSpecFail | kBatchKeyRange | kBatchOverflow))
+			if ((B.h_flags[d] & (kBatchSpecFail | kBatchKeyRange | kBatchOverflow))
+				&& !is_solo(offsets[d + 1] - offsets[d]))
 				fall.push_back(d);
 	}
 
@@ -1571,6 +1586,13 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		if (int e = pars_plan_load(B.helper, &pl->raw, sizeof pl->raw, &hp))
 			return fail(ctx, e, "helper plan load failed");
 		uint64_t s_cur = region_s[G], b_cur = 0;
+		// per-document records of these documents, written after they are all scanned
+		struct Rec {
+			uint32_t d, sbase, nstruct, cbase, nbr;
+			int32_t	 unclosed, balanced, well_formed, max_depth;
+		};
+		std::vector<Rec> recs;
+		recs.reserve(fall.size());
 		if (br) {
 			uint32_t dense = 0;	// dense brackets in use
 			CK(cudaMemcpyAsync(&dense, &B.bres->n_brackets, 4, cudaMemcpyDeviceToHost, st));
@@ -1600,17 +1622,21 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 				CK(cudaMemcpyAsync(static_cast<int32_t*>(B.ddepth.p) + b_cur, r.depth, r.n_brackets * 4,
 								   cudaMemcpyDeviceToDevice, st));
 			}
-			if (int e = set1<uint32_t>(ctx, B.sbase, d, static_cast<uint32_t>(s_cur), st)) return e;
-			if (int e = set1<uint32_t>(ctx, B.nstruct, d, static_cast<uint32_t>(r.n_struct), st)) return e;
-			if (int e = set1<uint32_t>(ctx, B.cbase, d, static_cast<uint32_t>(b_cur), st)) return e;
-			if (int e = set1<uint32_t>(ctx, B.nbr, d, static_cast<uint32_t>(r.n_brackets), st)) return e;
-			if (int e = set1<int32_t>(ctx, B.unclosed, d, r.unclosed_mode, st)) return e;
-			if (int e = set1<int32_t>(ctx, B.balanced, d, r.balanced, st)) return e;
-			if (int e = set1<int32_t>(ctx, B.well_formed, d, r.well_formed, st)) return e;
-			if (int e = set1<int32_t>(ctx, B.max_depth, d, r.max_depth, st)) return e;
+			recs.push_back({d, static_cast<uint32_t>(s_cur), static_cast<uint32_t>(r.n_struct),
+							static_cast<uint32_t>(b_cur), static_cast<uint32_t>(r.n_brackets), r.unclosed_mode,
+							r.balanced, r.well_formed, r.max_depth});
 			s_cur += r.n_struct;
 			b_cur += r.n_brackets;
 		}
+		for (const Rec& rc : recs) {
+			const void* src[9] = {&rc.sbase, &rc.nstruct, &rc.cbase, &rc.nbr, &rc.unclosed,
+								  &rc.balanced, &rc.well_formed, &rc.max_depth, nullptr};
+			DevBuf* dst[8] = {&B.sbase, &B.nstruct, &B.cbase, &B.nbr, &B.unclosed, &B.balanced, &B.well_formed,
+							  &B.max_depth};
+			for (int k = 0; k < 8; ++k)
+				CK(cudaMemcpyAsync(static_cast<uint32_t*>(dst[k]->p) + rc.d, src[k], 4, cudaMemcpyHostToDevice, st));
+		}
+		CK(cudaStreamSynchronize(st));	// `recs` is read by the copies above
 	}
 	CK(cudaStreamSynchronize(st));
 	out->structural	   = static_cast<const uint32_t*>(ctx->pos.p);
@@ -1626,7 +1652,8 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	out->balanced	   = run_pairs ? static_cast<const int32_t*>(B.balanced.p) : nullptr;
 	out->well_formed   = run_pairs ? static_cast<const int32_t*>(B.well_formed.p) : nullptr;
 	out->max_depth	   = run_pairs ? static_cast<const int32_t*>(B.max_depth.p) : nullptr;
-	out->n_recomputed  = static_cast<uint32_t>(fall.size());
+	out->n_recomputed  = static_cast<uint32_t>(fall.size() - solo.size());
+	out->n_whole_grid  = static_cast<uint32_t>(solo.size());
 	out->grid		   = static_cast<uint32_t>(G);
 	return 0;
 }
