@@ -276,6 +276,24 @@ int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_t* d_in, ui
                              uint32_t* d_struct, uint64_t cap, pars_noalloc_result* d_result,
                              void* stream);
 
+/* ---- autotuning ------------------------------------------------------------ */
+/* No counterpart in the reference.  The scan's launch parameter is the persistent
+ * grid size G, which is also its look-back depth (each tile folds the G - 1 tiles
+ * since its CTA's previous tile).  pars_autotune times the resident grid and 3/4,
+ * 2/3 and 1/2 of it on a sample document (device memory) and keeps the fastest for
+ * the plan's scan path and the sample's size bucket (floor(log2(n))); later scans
+ * of that path and bucket use it.  Results never depend on the grid.
+ * pars_tune_set sets the grid of a path and size bucket directly (0 = default). */
+typedef struct pars_tune_report {
+  uint32_t path, bucket, grid, n_candidates;
+  uint32_t cand_grid[8];
+  float cand_ms[8];
+} pars_tune_report;
+
+int pars_autotune(pars_ctx* ctx, int plan_id, const uint8_t* d_sample, uint64_t n,
+                  uint32_t flags, void* stream, pars_tune_report* out);
+int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid);
+
 /* ---- profiling ------------------------------------------------------------ */
 /* cf. stage_times (pipeline.cuh:746-748, 767-774, 998-1011): when enabled, the
  * context brackets its own launches with CUDA events on the caller's stream;

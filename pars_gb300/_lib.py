@@ -94,6 +94,12 @@ class ServerResult(ctypes.Structure):
                 ("start_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64)]
 
 
+class TuneReport(ctypes.Structure):
+    _fields_ = [("path", ctypes.c_uint32), ("bucket", ctypes.c_uint32), ("grid", ctypes.c_uint32),
+                ("n_candidates", ctypes.c_uint32), ("cand_grid", ctypes.c_uint32 * 8),
+                ("cand_ms", ctypes.c_float * 8)]
+
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "pars_version": (ctypes.c_int, []),
@@ -134,6 +140,9 @@ SIGNATURES = {
     "pars_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ServerResult)]),
     "pars_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ServerResult)]),
     "pars_server_release": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "pars_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(TuneReport)]),
+    "pars_tune_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32]),
     "pars_scan_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.c_void_p, ctypes.c_void_p]),

@@ -96,6 +96,9 @@ struct pars_ctx {
 	int				   num_sms	   = 0;
 	int				   scan_blocks[5] = {0, 0, 0, 0, 0};
 	int				   fast_blocks[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	uint64_t		   gen = 0;	 // bumped whenever a device buffer moves
+	// grid sizes chosen by pars_autotune / pars_tune_set: [path][log2 size bucket], 0 = default
+	int				   tuned_grid[5][48] = {};
 	std::string		   err;
 	std::vector<Plan*> plans;
 	unsigned int	   epoch = 0;
@@ -139,6 +142,17 @@ struct pars_ctx {
 		int		   blocks[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 		pars_ctx*  helper = nullptr;  // recomputes flagged documents on their own
 		std::vector<uint32_t> h_flags;
+		// pinned readback of the per-document flags and the result block
+		uint32_t*  h_pin	 = nullptr;
+		size_t	   h_pin_cap = 0;
+		DevResult* h_res	 = nullptr;
+		// captured launch graphs of the batch's device work, by layout
+		struct GraphEntry {
+			uint64_t		key[12];
+			cudaGraphExec_t exec;
+			uint64_t		launches;
+		};
+		std::vector<GraphEntry> graphs;
 	} batch;
 };
 
@@ -194,6 +208,7 @@ int grow_impl(pars_ctx* ctx, DevBuf& b, size_t bytes, const char* what) {
 		return cuda_fail(ctx, e, msg);
 	}
 	b.cap = want;
+	ctx->gen++;	 // captured launch graphs hold the old pointers
 	ctx->arena_used += want;
 	return 0;
 }
@@ -445,6 +460,14 @@ int make_row_map(pars_ctx* ctx, const uint8_t* base, uint64_t rows, CUtensorMap*
 	return 0;
 }
 
+// Size bucket of a document for tuned launch parameters: floor(log2(n)).
+int size_bucket(uint64_t n) {
+	int b = 0;
+	while (b < 47 && (n >> (b + 1)))
+		++b;
+	return b;
+}
+
 // `first` = first launch of a document: clears the result block + key histogram.
 int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true) {
 	const uint64_t o	 = reinterpret_cast<uintptr_t>(s.d_in) & 15u;
@@ -498,7 +521,11 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	void* args[] = {&a};
 	if (fast && use_ws(s.path)) {
 		const bool	br	 = br_kernel;
-		const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
+		int			g	 = ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)];
+		const int	tg	 = ctx->tuned_grid[s.path][size_bucket(s.n)];
+		if (tg > 0 && tg < g)
+			g = tg;
+		const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, static_cast<uint64_t>(g)));
 		WsArgs		wa {a, total / 128};
 		CUtensorMap map;
 		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
@@ -866,6 +893,11 @@ int pars_destroy(pars_ctx* ctx) {
 			cudaFree(B.bres);
 		if (B.helper)
 			pars_destroy(B.helper);
+		for (auto& g : B.graphs) cudaGraphExecDestroy(g.exec);
+		if (B.h_pin)
+			cudaFreeHost(B.h_pin);
+		if (B.h_res)
+			cudaFreeHost(B.h_res);
 	}
 	if (ctx->ctr) cudaFree(ctx->ctr);
 	if (ctx->rb) cudaFree(ctx->rb);
@@ -1238,14 +1270,21 @@ int ensure_batch_config(pars_ctx* ctx, int path, bool br) {
 
 // LSD sort of `n_cap` int32 keys (count in res->n_brackets, minimum res->min_key) in
 // 8-bit digits; the stable order of indices lands in `order`.
-int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint32_t* order, uint64_t n_cap,
-			 DevResult* res, int passes, cudaStream_t st) {
+int lsd_sort_prepare(pars_ctx* ctx, uint64_t n_cap) {
 	const uint64_t ntiles_sort = (n_cap + sort_tile_keys() - 1) / sort_tile_keys() + 1;
 	if (int e = grow(ctx, ctx->lb, ntiles_sort * 256 * sizeof(uint64_t)))
 		return e;
 	if (int e = grow(ctx, ctx->digit_hist, 256 * 4))
 		return e;
-	if (int e = grow(ctx, ctx->sort_keys_a, n_cap * 4 + 16))
+	return grow(ctx, ctx->sort_keys_a, n_cap * 4 + 16);
+}
+
+// clear_lb: clear the look-back words before every pass (a replayed graph repeats
+// its passes' epochs, so words of the previous replay must not be read as current).
+int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint32_t* order, uint64_t n_cap,
+			 DevResult* res, int passes, cudaStream_t st, bool clear_lb, uint64_t& launches) {
+	const uint64_t ntiles_sort = (n_cap + sort_tile_keys() - 1) / sort_tile_keys() + 1;
+	if (int e = lsd_sort_prepare(ctx, n_cap))
 		return e;
 	const int32_t*	kin	 = keys;
 	const uint32_t* iin	 = nullptr;
@@ -1254,9 +1293,11 @@ int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint
 	int				out		= (passes % 2 == 1) ? 0 : 1;
 	for (int ps = 0; ps < passes; ++ps) {
 		CK(cudaMemsetAsync(ctx->digit_hist.p, 0, 256 * 4, st));
+		if (clear_lb)
+			CK(cudaMemsetAsync(ctx->lb.p, 0, ntiles_sort * 256 * sizeof(uint64_t), st));
 		k_digit_hist<<<ctx->num_sms * 4, 256, 0, st>>>(kin, res, 8u * ps, static_cast<unsigned int*>(ctx->digit_hist.p));
 		CK(cudaGetLastError());
-		ctx->launches++;
+		launches++;
 		SortPass sp {};
 		sp.keys_in	  = kin;
 		sp.idx_in	  = iin;
@@ -1273,7 +1314,7 @@ int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint
 		sp.first	  = 0;
 		void* a1[]	  = {&sp};
 		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4), dim3(256), a1, 0, st));
-		ctx->launches++;
+		launches++;
 		kin = kbuf[out];
 		iin = ibuf[out];
 		out ^= 1;
@@ -1439,14 +1480,19 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	}
 	if (!B.bres)
 		CK(cudaMalloc(&B.bres, sizeof(DevResult)));
-	for (DevBuf* b : {&B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.flags, &B.cbase, &B.sbase, &B.bbase,
-					  &B.balanced, &B.well_formed, &B.max_depth})
-		CK(cudaMemsetAsync(b->p, 0, nd * 4, st));
-	CK(cudaMemsetAsync(B.minbal.p, 0, nd * 8, st));
-	CK(cudaMemsetAsync(B.maxbal.p, 0, nd * 8, st));
-	CK(cudaMemsetAsync(B.cta_bcount.p, 0, static_cast<size_t>(G) * 4, st));
-	CK(cudaMemsetAsync(B.bres, 0, sizeof(DevResult), st));
-	CK(cudaMemsetAsync(ctx->rb, 0, sizeof(ResBlock), st));
+	if (run_pairs && br)
+		if (int e = lsd_sort_prepare(ctx, cap_b))
+			return e;
+	if (B.h_pin_cap < nd) {
+		if (B.h_pin)
+			cudaFreeHost(B.h_pin);
+		B.h_pin		= nullptr;
+		B.h_pin_cap = 0;
+		CK(cudaHostAlloc(reinterpret_cast<void**>(&B.h_pin), nd * 4 + 1024, cudaHostAllocDefault));
+		B.h_pin_cap = nd + 256;
+	}
+	if (!B.h_res)
+		CK(cudaHostAlloc(reinterpret_cast<void**>(&B.h_res), sizeof(DevResult), cudaHostAllocDefault));
 
 	BatchDesc bd {};
 	bd.doc_start  = static_cast<const uint64_t*>(B.doc_start.p);
@@ -1493,10 +1539,22 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		CUtensorMap map;
 		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
 			return r;
-		void* wargs[] = {&wa, &map};
+		void*	 wargs[] = {&wa, &map};
+		uint64_t nl		 = 0;  // kernels of the sequence
+		// The batch's device work: every size and pointer in it follows from the
+		// layout key below, every count it reads lives in device memory.
+		auto launch_all = [&](bool clear_lb) -> int {
+		for (DevBuf* b : {&B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.flags, &B.cbase, &B.sbase,
+						  &B.bbase, &B.balanced, &B.well_formed, &B.max_depth})
+			CK(cudaMemsetAsync(b->p, 0, nd * 4, st));
+		CK(cudaMemsetAsync(B.minbal.p, 0, nd * 8, st));
+		CK(cudaMemsetAsync(B.maxbal.p, 0, nd * 8, st));
+		CK(cudaMemsetAsync(B.cta_bcount.p, 0, static_cast<size_t>(G) * 4, st));
+		CK(cudaMemsetAsync(B.bres, 0, sizeof(DevResult), st));
+		CK(cudaMemsetAsync(ctx->rb, 0, sizeof(ResBlock), st));
 		CK(cudaLaunchKernel(scan_ws_batch_kernel(path, br), dim3(G), dim3(scan_ws_threads()), wargs,
 							scan_ws_smem_bytes(), st));
-		ctx->launches++;
+		nl++;
 		if (br) {
 			BatchR6 r6 {};
 			r6.doc_start   = bd.doc_start;
@@ -1535,15 +1593,15 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			const int grid = ctx->num_sms * 4;
 			CK(cudaLaunchKernel(batch_kernel(0), dim3(grid), dim3(256), ra, 0, st));	 // compact
 			CK(cudaLaunchKernel(batch_kernel(1), dim3(grid), dim3(256), ra, 0, st));	 // docs
-			ctx->launches += 2;
+			nl += 2;
 			if (run_pairs) {
 				if (int e = lsd_sort(ctx, static_cast<const int32_t*>(B.dkey.p), static_cast<int32_t*>(B.dkey_b.p),
 									 static_cast<uint32_t*>(B.order_b.p), static_cast<uint32_t*>(B.order.p), cap_b,
-									 B.bres, 4, st))
+									 B.bres, 4, st, clear_lb, nl))
 					return e;
 				CK(cudaLaunchKernel(batch_kernel(2), dim3(grid), dim3(256), ra, 0, st));	 // segments
 				CK(cudaLaunchKernel(batch_kernel(3), dim3(grid), dim3(256), ra, 0, st));	 // pairs
-				ctx->launches += 2;
+				nl += 2;
 			}
 		}
 		if (run_pairs) {
@@ -1559,14 +1617,68 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			r6.max_depth   = static_cast<int32_t*>(B.max_depth.p);
 			void* ra[]	   = {&r6};
 			CK(cudaLaunchKernel(batch_kernel(4), dim3(ctx->num_sms * 4), dim3(256), ra, 0, st));	 // flags
-			ctx->launches++;
+			nl++;
 		}
-		// which documents need recomputing
-		B.h_flags.assign(nd, 0);
-		CK(cudaMemcpyAsync(B.h_flags.data(), B.flags.p, nd * 4, cudaMemcpyDeviceToHost, st));
-		DevResult hr {};
-		CK(cudaMemcpyAsync(&hr, ctx->res, sizeof hr, cudaMemcpyDeviceToHost, st));
+		// which documents need recomputing, and the error word
+		CK(cudaMemcpyAsync(B.h_pin, B.flags.p, nd * 4, cudaMemcpyDeviceToHost, st));
+		CK(cudaMemcpyAsync(B.h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+		return 0;
+		};
+		// Replay a captured graph of this layout, or capture one (a capturable stream:
+		// not the legacy default stream).
+		const uint64_t key[12] = {reinterpret_cast<uintptr_t>(pl), static_cast<uint64_t>(path), br ? 1u : 0u, flags,
+								  static_cast<uint64_t>(G), ndocs, cap_s, cap_b, ctx->gen,
+								  reinterpret_cast<uintptr_t>(B.h_pin), reinterpret_cast<uintptr_t>(base), total};
+		bool done = false;
+		if (st != nullptr) {
+			for (auto& g : B.graphs)
+				if (std::memcmp(g.key, key, sizeof key) == 0) {
+					CK(cudaGraphLaunch(g.exec, st));
+					ctx->launches += g.launches;
+					done = true;
+					break;
+				}
+			if (!done) {
+				CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+				const int	rc = launch_all(true);
+				cudaGraph_t graph = nullptr;
+				const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+				if (rc) {
+					if (graph)
+						cudaGraphDestroy(graph);
+					return rc;
+				}
+				cudaGraphExec_t exec = nullptr;
+				if (ec == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+					cudaGraphDestroy(graph);
+					if (B.graphs.size() >= 8) {
+						cudaGraphExecDestroy(B.graphs.front().exec);
+						B.graphs.erase(B.graphs.begin());
+					}
+					pars_ctx::Batch::GraphEntry ge {};
+					std::memcpy(ge.key, key, sizeof key);
+					ge.exec		= exec;
+					ge.launches = nl;
+					B.graphs.push_back(ge);
+					CK(cudaGraphLaunch(exec, st));
+					ctx->launches += nl;
+					done = true;
+				} else {
+					if (graph)
+						cudaGraphDestroy(graph);
+					cudaGetLastError();	 // capture unavailable: run the sequence directly
+				}
+			}
+		}
+		if (!done) {
+			nl = 0;
+			if (int rc = launch_all(false))
+				return rc;
+			ctx->launches += nl;
+		}
 		CK(cudaStreamSynchronize(st));
+		B.h_flags.assign(B.h_pin, B.h_pin + nd);
+		const DevResult hr = *B.h_res;
 		if (hr.error) {
 			reset_after_error(ctx, st);
 			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
@@ -1655,5 +1767,88 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	out->n_recomputed  = static_cast<uint32_t>(fall.size() - solo.size());
 	out->n_whole_grid  = static_cast<uint32_t>(solo.size());
 	out->grid		   = static_cast<uint32_t>(G);
+	return 0;
+}
+
+// ================================================================================
+// Autotuning
+// ================================================================================
+extern "C" int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl)
+		return ctx ? fail(ctx, PARS_EINVAL, "bad plan id") : PARS_EINVAL;
+	if (pl->path < 0 || pl->path > 4)
+		return fail(ctx, PARS_EINVAL, "bad path");
+	ctx->tuned_grid[pl->path][size_bucket(n)] = static_cast<int>(grid);
+	return 0;
+}
+
+extern "C" int pars_autotune(pars_ctx* ctx, int plan_id, const uint8_t* d_sample, uint64_t n, uint32_t flags,
+							 void* stream, pars_tune_report* out) {
+	Plan* pl = get_plan(ctx, plan_id);
+	if (!pl || !out || !n || !d_sample)
+		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	cudaSetDevice(ctx->device);
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	std::memset(out, 0, sizeof *out);
+	const int path	 = pl->path;
+	const int bucket = size_bucket(n);
+	out->path		 = static_cast<uint32_t>(path);
+	out->bucket		 = static_cast<uint32_t>(bucket);
+	if (!use_ws(path)) {
+		out->grid = 0;	// the general kernel's grid is set by occupancy
+		return 0;
+	}
+	const bool br = pl->host.has_brackets != 0;
+	if (int r = ensure_fast_config(ctx, path, br))
+		return r;
+	const int full = ctx->fast_blocks[path * 2 + (br ? 1 : 0)];
+	// candidates: the whole resident grid and fractions of it (look-back window G - 1)
+	int cands[8], nc = 0;
+	for (int div : {4, 3, 2}) {
+		const int g = full * (div - 1) / div;
+		if (g >= 1)
+			cands[nc++] = g;
+	}
+	cands[nc++] = full;
+	cudaEvent_t e0, e1;
+	CK(cudaEventCreate(&e0));
+	CK(cudaEventCreate(&e1));
+	const int saved = ctx->tuned_grid[path][bucket];
+	float	  best	= 0;
+	int		  bestg = full;
+	for (int i = 0; i < nc; ++i) {
+		ctx->tuned_grid[path][bucket] = cands[i];
+		pars_device_result r {};
+		for (int w = 0; w < 2; ++w)
+			if (int e = scan_device_impl(ctx, pl, d_sample, n, flags, st, &r)) {
+				ctx->tuned_grid[path][bucket] = saved;
+				return e;
+			}
+		float ms = 1e30f;
+		for (int rep = 0; rep < 3; ++rep) {
+			CK(cudaEventRecord(e0, st));
+			if (int e = scan_device_impl(ctx, pl, d_sample, n, flags, st, &r)) {
+				ctx->tuned_grid[path][bucket] = saved;
+				return e;
+			}
+			CK(cudaEventRecord(e1, st));
+			CK(cudaEventSynchronize(e1));
+			float t = 0;
+			CK(cudaEventElapsedTime(&t, e0, e1));
+			ms = std::min(ms, t);
+		}
+		out->cand_grid[i] = static_cast<uint32_t>(cands[i]);
+		out->cand_ms[i]	  = ms;
+		if (i == 0 || ms < best) {
+			best  = ms;
+			bestg = cands[i];
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	out->n_candidates			  = static_cast<uint32_t>(nc);
+	out->grid					  = static_cast<uint32_t>(bestg);
+	ctx->tuned_grid[path][bucket] = bestg;
 	return 0;
 }

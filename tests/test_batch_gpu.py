@@ -93,3 +93,32 @@ def test_batch_empty(ctx):
     sc = Scanner(plan_bytes("json"), ctx=ctx)
     bv = sc.scan_batch(0, np.zeros(1, np.uint64))
     assert bv.ndocs == 0
+
+
+def test_batch_graph_replay(ctx):
+    """On a non-default stream the batch's device work is captured once per layout
+    and replayed: a second batch with the same layout and new bytes must come out
+    right (no state of the first replay may leak into the second)."""
+    sc = Scanner(plan_bytes("json"), ctx=ctx)
+    stream = torch.cuda.Stream()
+    docs_a = lognormal_docs(13, 300, synth.json_doc, median=1500, sigma=1.0)
+    sizes = [d.size for d in docs_a]
+    docs_b = [synth.json_doc(99_000 + i, s)[:s] for i, s in enumerate(sizes)]
+    docs_b = [d if d.size == s else np.pad(d, (0, s - d.size), constant_values=32) for d, s in zip(docs_b, sizes)]
+    buf = torch.empty(sum(sizes), dtype=torch.uint8, device="cuda")  # one input buffer: one layout
+    for docs in (docs_a, docs_b, docs_a):
+        data, offs = concat(docs)
+        buf.copy_(torch.from_numpy(data))
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            bv = sc.scan_batch(buf.data_ptr(), offs, stream=stream.cuda_stream, want_pairs=True)
+        stream.synchronize()
+        for d, doc in enumerate(docs):
+            t = torch.from_numpy(doc).cuda()
+            r = sc.scan_device(t.data_ptr(), doc.size, want_pairs=True)
+            torch.cuda.synchronize()
+            e = r.to_numpy()
+            got = bv.doc(d)
+            assert np.array_equal(got["pos"], e["pos"]) and np.array_equal(got["pair"], e["pair"]), d
+            assert (got["balanced"], got["well_formed"], got["max_depth"]) == \
+                (int(r.balanced), int(r.well_formed), r.max_depth), d
