@@ -162,6 +162,21 @@ def cpu_baseline(plan_bytes: bytes, data: np.ndarray, budget_s: float = 10.0):
                       f"{t_total:.1f} s; the reference scan is sequential per document"}
 
 
+def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's time (ms): replicas finish when the last one does."""
+    if dist is None:
+        return ms
+    import torch
+    x = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def whole_job_gbps(n_bytes_per_rank: int, world: int, t_max_ms: float) -> float:
+    """Whole-job throughput: every rank's bytes over the slowest rank's time."""
+    return world * n_bytes_per_rank / (t_max_ms / 1e3) / 1e9
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -399,12 +414,8 @@ def main():
                                                   barrier)
     clocks = clk.summary()
     # whole-job throughput: all ranks' bytes over the slowest rank's time
-    t_max = ms
-    if dist is not None:
-        x = torch.tensor([ms], device="cuda")
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        t_max = float(x.item())
-    value = world * n / (t_max / 1e3) / 1e9
+    t_max = max_over_ranks(ms, dist, device="cuda")
+    value = whole_job_gbps(n, world, t_max)
     alg_bytes = n + 4 * r.n_struct
     achieved = alg_bytes / (scan_ms / 1e3) / 1e9
 
