@@ -1,6 +1,7 @@
 """Run the scan a few times on one seeded synthetic document, for profilers.
 
     python -m pars_gb300.profile_run <csv|json> <MiB> [repeats] [--pairs]
+    python -m pars_gb300.profile_run batch <documents> [repeats]
 
 Loads the plan from tests/golden/plans, generates the document with the library's
 seeded generators, scans it `repeats` times on the current CUDA device and prints
@@ -17,6 +18,19 @@ def main(argv):
     repeats = int(argv[2]) if len(argv) > 2 and not argv[2].startswith("-") else 3
     pairs = "--pairs" in argv
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if grammar == "batch":
+        # `mib` documents of the batched JSON workload (log-normal sizes, median 2 KiB)
+        with open(os.path.join(root, "tests", "golden", "plans", "json.plan"), "rb") as f:
+            plan = f.read()
+        data, offs = synth.json_batch(20261203, mib)
+        t = torch.from_numpy(data).cuda()
+        sc = Scanner(plan)
+        s = torch.cuda.Stream()
+        for _ in range(repeats):
+            r = sc.scan_batch(t.data_ptr(), offs, stream=s.cuda_stream, want_pairs=True, host_view=False)
+        torch.cuda.synchronize()
+        print("batch", data.size, mib, r.n_recomputed)
+        return
     with open(os.path.join(root, "tests", "golden", "plans", f"{grammar}.plan"), "rb") as f:
         plan = f.read()
     data = synth.csv_doc(7, mib << 20) if grammar == "csv" else synth.json_doc(7, mib << 20)
