@@ -149,6 +149,31 @@ def test_json_64mib_config(scanners):
     assert g["path"] == "escape"
 
 
+def test_json_deep_2gib_config(scanners):
+    """The deep-nesting JSON stress at its full 2 GiB size (depth up to 1024, a fifth
+    of the bytes in 1-64 KiB strings with escape runs): every output against the
+    oracle, plus size-independent properties of the pairs."""
+    plan = plan_bytes("json")
+    data = synth.json_deep(2, 2 << 30)
+    assert data.size >= 2 << 30
+    buf, ptr = to_dev(data)
+    r = scanners["json"].scan_device(ptr, data.size, want_pairs=True)
+    torch.cuda.synchronize()
+    g = r.to_numpy()
+    del buf
+    sr = oracle.scan(plan, data)
+    assert np.array_equal(g["pos"], sr.positions), "offsets"
+    assert np.array_equal(g["bpos"], sr.bracket_pos), "bracket offsets"
+    pr = oracle.pair(plan, sr.bracket_char)
+    assert np.array_equal(g["depth"], pr.depth), "depth keys"
+    assert np.array_equal(g["bpair"], pr.pair), "pairs"
+    assert (r.balanced, r.well_formed, r.max_depth) == (pr.balanced, pr.well_formed, pr.max_depth)
+    assert r.max_depth > 500                       # the stress really nests deep
+    bp = g["bpair"]
+    has = bp >= 0
+    assert np.array_equal(bp[bp[has]], np.nonzero(has)[0])  # pairing is an involution
+
+
 def test_csv_full_size_properties(scanners):
     """1 GiB CSV: size-independent properties, and exact equality with the oracle."""
     plan = plan_bytes("csv")
