@@ -122,6 +122,14 @@ struct pars_ctx {
 	uint8_t*	   h_chars = nullptr;
 	int32_t*	   h_pair = nullptr;
 	size_t		   h_out_cap = 0;
+	// pipelined host path: copy-in stream, copy-out stream, one event pair per chunk
+	struct Pipe {
+		bool		 ready = false;
+		cudaStream_t in_st = nullptr, out_st = nullptr;
+		cudaEvent_t	 start = nullptr;
+		cudaEvent_t	 in_ev[32] = {}, scan_ev[32] = {};
+		DevCarry*	 h_carry = nullptr;	 // pinned: each chunk's carry after its scan
+	} pipe;
 	// chunk state
 	uint64_t chunk_index = 0;
 	cudaEvent_t ev = nullptr;
@@ -817,6 +825,187 @@ int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, u
 	return fail(ctx, PARS_ECUDA, "scan did not converge");
 }
 
+// Pinned host copies of the outputs, grown to `need` entries; the first `keep`
+// structural offsets (and chars) already copied home move to the new buffers.
+int grow_host_out(pars_ctx* ctx, size_t need, size_t keep, bool chars) {
+	if (need <= ctx->h_out_cap)
+		return 0;
+	const size_t cap = need + need / 2 + 1024;
+	uint32_t*	 pos = nullptr;
+	uint8_t*	 chr = nullptr;
+	int32_t*	 pr	 = nullptr;
+	CK(cudaHostAlloc(&pos, cap * 4, cudaHostAllocDefault));
+	CK(cudaHostAlloc(&chr, cap, cudaHostAllocDefault));
+	CK(cudaHostAlloc(&pr, cap * 4, cudaHostAllocDefault));
+	if (keep) {
+		std::memcpy(pos, ctx->h_pos, keep * 4);
+		if (chars)
+			std::memcpy(chr, ctx->h_chars, keep);
+	}
+	if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
+	if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
+	if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
+	ctx->h_pos	   = pos;
+	ctx->h_chars   = chr;
+	ctx->h_pair	   = pr;
+	ctx->h_out_cap = cap;
+	return 0;
+}
+
+constexpr int	   kPipeChunks	   = 32;
+constexpr uint64_t kPipeMinChunk   = 4ull << 20;
+constexpr uint64_t kPipeMinBytes   = 8ull << 20;
+
+int pipe_setup(pars_ctx* ctx) {
+	auto& P = ctx->pipe;
+	if (P.ready)
+		return 0;
+	if (!P.in_st)
+		CK(cudaStreamCreateWithFlags(&P.in_st, cudaStreamNonBlocking));
+	if (!P.out_st)
+		CK(cudaStreamCreateWithFlags(&P.out_st, cudaStreamNonBlocking));
+	if (!P.start)
+		CK(cudaEventCreateWithFlags(&P.start, cudaEventDisableTiming));
+	for (int i = 0; i < kPipeChunks; ++i) {
+		if (!P.in_ev[i])
+			CK(cudaEventCreateWithFlags(&P.in_ev[i], cudaEventDisableTiming));
+		if (!P.scan_ev[i])
+			CK(cudaEventCreateWithFlags(&P.scan_ev[i], cudaEventDisableTiming));
+	}
+	if (!P.h_carry)
+		CK(cudaHostAlloc(&P.h_carry, kPipeChunks * sizeof(DevCarry), cudaHostAllocDefault));
+	P.ready = true;
+	return 0;
+}
+
+// Whether a pinned host document takes the pipelined path: a bracket-aware or
+// bracket-less fast path (the escape path may need a whole-document rescan under
+// exact descriptor semantics), no per-byte bitmap, no stage timing.
+bool pipe_applies(const pars_ctx* ctx, const Plan* pl, uint64_t n, uint32_t flags) {
+	return n >= kPipeMinBytes && n < (1ull << 32) && !ctx->profiling && use_ws(pl->path) && pl->path != kPathEscape
+		&& !(flags & (PARS_WANT_MASK | PARS_FORCE_GENERIC));
+}
+
+// The pipelined host path (pars_scan_host, pinned input).  The document crosses to
+// the device in up to 32 chunks on a copy-in stream; chunk i is scanned on the
+// caller's stream as soon as its bytes have landed, its carry joining it to chunk
+// i-1 exactly like pars_scan_chunk; once chunk i's scan has finished the host reads
+// its running structural count and sends that chunk's offsets (and chars) home on a
+// copy-out stream while later chunks are still crossing.  R6 runs after the last
+// chunk; pair_pos follows it.  `*redo` = outputs overflowed the reserved capacity:
+// the document is resident and the caller reruns it on the whole-document path.
+int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n, uint32_t flags,
+						cudaStream_t st, pars_host_result* out, bool* redo) {
+	*redo = false;
+	if (int r = pipe_setup(ctx))
+		return r;
+	auto&		   P		 = ctx->pipe;
+	const bool	   run_pairs = (flags & PARS_RUN_PAIRS) && pl->host.has_brackets;
+	const bool	   chars	 = (flags & PARS_WANT_CHARS) != 0;
+	const uint64_t align	 = 64ull << 10;
+	const uint64_t chunk	 = std::max(kPipeMinChunk, ((n + kPipeChunks - 1) / kPipeChunks + align - 1) / align * align);
+	const int	   nch		 = static_cast<int>((n + chunk - 1) / chunk);
+	const uint64_t want_s	 = std::max<uint64_t>(ctx->cap_s, n / 3 + 4096);
+	const uint64_t want_b	 = std::max<uint64_t>(ctx->cap_b, pl->host.has_brackets ? n / 6 + 4096 : 1024);
+	if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
+		return r;
+	uint8_t* d = static_cast<uint8_t*>(ctx->d_in.p);
+	// everything before this call on the caller's stream precedes the copies
+	CK(cudaEventRecord(P.start, st));
+	CK(cudaStreamWaitEvent(P.in_st, P.start, 0));
+	CK(cudaStreamWaitEvent(P.out_st, P.start, 0));
+	for (int i = 0; i < nch; ++i) {
+		const uint64_t off = i * chunk, len = std::min(chunk, n - off);
+		CK(cudaMemcpyAsync(d + off, h_in + off, len, cudaMemcpyHostToDevice, P.in_st));
+		CK(cudaEventRecord(P.in_ev[i], P.in_st));
+	}
+	// fast paths start from a zero carry
+	CK(cudaMemsetAsync(ctx->carry, 0, sizeof(DevCarry), st));
+	ctx->cur_in = nullptr;	// the chunk scans write the bracket bytes themselves
+	const uint32_t sflags = (flags & (PARS_WANT_PAIRS | PARS_WANT_CHARS)) | kScanOwnBchar;
+	for (int i = 0; i < nch; ++i) {
+		const uint64_t off = i * chunk, len = std::min(chunk, n - off);
+		DevCarry*	   cin	= ctx->carry + (i & 1);
+		DevCarry*	   cout = ctx->carry + ((i + 1) & 1);
+		CK(cudaStreamWaitEvent(st, P.in_ev[i], 0));
+		Scan s {d + off, len, sflags, st, pl->path, cin, cout};
+		if (int r = launch_scan(ctx, pl, s, i == 0))
+			return r;
+		CK(cudaMemcpyAsync(P.h_carry + i, cout, sizeof(DevCarry), cudaMemcpyDeviceToHost, st));
+		CK(cudaEventRecord(P.scan_ev[i], st));
+	}
+	if (run_pairs)
+		if (int r = launch_pairs_speculative(ctx, pl, flags, st))
+			return r;
+	CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+	// offsets of each scanned chunk go home while later chunks cross and scan
+	uint64_t prev = 0;
+	bool	 over = false;
+	for (int i = 0; i < nch && !over; ++i) {
+		CK(cudaEventSynchronize(P.scan_ev[i]));
+		const uint64_t ns = P.h_carry[i].ns;
+		if (ns > ctx->cap_s) {
+			over = true;
+			break;
+		}
+		if (ns > ctx->h_out_cap) {
+			// size the host copies for the whole document from the density so far
+			const uint64_t covered = std::min(n, (i + 1) * chunk);
+			const uint64_t est	   = static_cast<uint64_t>(static_cast<double>(ns) / covered * n * 1.05);
+			CK(cudaStreamSynchronize(P.out_st));
+			if (int r = grow_host_out(ctx, std::max(ns, est), prev, chars))
+				return r;
+		}
+		if (ns > prev) {
+			CK(cudaMemcpyAsync(ctx->h_pos + prev, static_cast<const uint32_t*>(ctx->pos.p) + prev,
+							   (ns - prev) * 4, cudaMemcpyDeviceToHost, P.out_st));
+			if (chars)
+				CK(cudaMemcpyAsync(ctx->h_chars + prev, static_cast<const uint8_t*>(ctx->chars.p) + prev,
+								   ns - prev, cudaMemcpyDeviceToHost, P.out_st));
+		}
+		prev = ns;
+	}
+	CK(cudaStreamSynchronize(st));
+	CK(cudaStreamSynchronize(P.out_st));
+	DevResult r = *ctx->h_res;
+	if (r.error) {
+		reset_after_error(ctx, st);
+		return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+	}
+	if (over || r.n_struct > ctx->cap_s || r.n_brackets > ctx->cap_b) {
+		*redo = true;
+		return 0;
+	}
+	if (run_pairs && !r.sort_ok) {
+		if (int e = pairs_fallback(ctx, pl, flags, st, r))
+			return e;
+		CK(cudaMemcpyAsync(ctx->h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		r = *ctx->h_res;
+		if (r.error) {
+			reset_after_error(ctx, st);
+			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
+		}
+	}
+	if (int e = grow_host_out(ctx, r.n_struct, prev, chars))
+		return e;
+	if ((flags & PARS_WANT_PAIRS) && r.n_struct) {
+		CK(cudaMemcpyAsync(ctx->h_pair, ctx->pair.p, r.n_struct * 4, cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+	}
+	pars_device_result dr {};
+	fill_result(ctx, r, flags, run_pairs, &dr);
+	out->structural	   = ctx->h_pos;
+	out->chars		   = chars ? ctx->h_chars : nullptr;
+	out->pair_pos	   = (flags & PARS_WANT_PAIRS) ? ctx->h_pair : nullptr;
+	out->n_struct	   = dr.n_struct;
+	out->balanced	   = dr.balanced;
+	out->well_formed   = dr.well_formed;
+	out->max_depth	   = dr.max_depth;
+	out->unclosed_mode = dr.unclosed_mode;
+	return 0;
+}
+
 }  // namespace
 
 // ================================================================================
@@ -908,6 +1097,17 @@ int pars_destroy(pars_ctx* ctx) {
 	if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
 	if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
 	if (ctx->ev) cudaEventDestroy(ctx->ev);
+	{
+		auto& P = ctx->pipe;
+		if (P.in_st) cudaStreamDestroy(P.in_st);
+		if (P.out_st) cudaStreamDestroy(P.out_st);
+		if (P.start) cudaEventDestroy(P.start);
+		for (int i = 0; i < 32; ++i) {
+			if (P.in_ev[i]) cudaEventDestroy(P.in_ev[i]);
+			if (P.scan_ev[i]) cudaEventDestroy(P.scan_ev[i]);
+		}
+		if (P.h_carry) cudaFreeHost(P.h_carry);
+	}
 	for (cudaEvent_t& e : ctx->prof)
 		if (e)
 			cudaEventDestroy(e);
@@ -978,7 +1178,16 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 	const bool pinned = cudaPointerGetAttributes(&attr, h_in) == cudaSuccess
 					 && (attr.type == cudaMemoryTypeHost);
 	cudaGetLastError();
-	if (n) {
+	bool resident = false;
+	if (pinned && pipe_applies(ctx, pl, n, flags)) {
+		bool redo = false;
+		if (int r = scan_host_pipelined(ctx, pl, h_in, n, flags, st, out, &redo))
+			return r;
+		if (!redo)
+			return 0;
+		resident = true;  // outputs overflowed: rerun the resident document below
+	}
+	if (n && !resident) {
 		if (pinned) {
 			CK(cudaMemcpyAsync(ctx->d_in.p, h_in, n, cudaMemcpyHostToDevice, st));
 		} else {
@@ -1002,19 +1211,8 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 	if (int r = scan_device_impl(ctx, pl, static_cast<const uint8_t*>(ctx->d_in.p), n, flags, st, &dr))
 		return r;
 	const size_t need = dr.n_struct;
-	if (need > ctx->h_out_cap) {
-		if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
-		if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
-		if (ctx->h_pair) cudaFreeHost(ctx->h_pair);
-		ctx->h_pos = nullptr;
-		ctx->h_chars = nullptr;
-		ctx->h_pair = nullptr;
-		const size_t cap = need + need / 2 + 1024;
-		CK(cudaHostAlloc(&ctx->h_pos, cap * 4, cudaHostAllocDefault));
-		CK(cudaHostAlloc(&ctx->h_chars, cap, cudaHostAllocDefault));
-		CK(cudaHostAlloc(&ctx->h_pair, cap * 4, cudaHostAllocDefault));
-		ctx->h_out_cap = cap;
-	}
+	if (int r = grow_host_out(ctx, need, 0, false))
+		return r;
 	if (need) {
 		CK(cudaMemcpyAsync(ctx->h_pos, dr.structural, need * 4, cudaMemcpyDeviceToHost, st));
 		if (dr.chars)

@@ -196,6 +196,41 @@ def test_scan_host_matches_device(scanners):
     assert (h.unclosed_mode, h.balanced, h.well_formed, h.max_depth) == e["meta"]
 
 
+@pytest.mark.parametrize("grammar", GRAMMARS)
+def test_scan_host_pipelined(grammar):
+    """Pinned input of 20 MiB + 5 bytes (five 4 MiB chunks and a ragged end) through
+    pars_scan_host, which pipelines copy-in, chunk scans and copy-out on the fast
+    paths: offsets, chars, pairs and flags against the oracle.  A fresh context, so
+    the host copies grow while the document is in flight."""
+    from tests_alphabets import ALPHABETS
+    plan = plan_bytes(grammar)
+    data = synth.alpha(4099, ALPHABETS[grammar], (20 << 20) + 5)
+    pinned = torch.from_numpy(data).pin_memory()
+    e = expected_from_oracle(plan, data)
+    sc = Scanner(plan, ctx=Context(0))
+    for _ in range(2):  # the second run reuses the grown buffers
+        h = sc.scan_host(pinned.numpy(), want_pairs=True, want_chars=True)
+        assert np.array_equal(h.structural, e["pos"])
+        assert np.array_equal(h.chars, e["chars"])
+        assert np.array_equal(h.pair_pos, e["pair"])
+        assert (h.unclosed_mode, h.balanced, h.well_formed, h.max_depth) == e["meta"]
+
+
+def test_scan_host_pipelined_overflow():
+    """A CSV document of delimiters only has a structural at every byte, more than the
+    pipelined path reserves: it reruns the resident document on the whole-document
+    path and still returns every offset."""
+    n = (12 << 20) + 3
+    data = np.full(n, ord(","), np.uint8)
+    data[::7] = ord("a")
+    pinned = torch.from_numpy(data).pin_memory()
+    sc = Scanner(plan_bytes("csv"), ctx=Context(0))
+    h = sc.scan_host(pinned.numpy(), want_chars=True)
+    pos = np.nonzero(data == ord(","))[0].astype(np.uint32)
+    assert np.array_equal(h.structural, pos)
+    assert np.all(h.chars == ord(","))
+
+
 @pytest.mark.parametrize("grammar", ["json", "csv", "toml", "xml"])
 def test_chunked_equals_whole(ctx, grammar):
     plan = plan_bytes(grammar)
