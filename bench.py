@@ -446,7 +446,8 @@ def main():
     e2e = {"value": round(world * n / e2e_s / 1e9, 3), "unit": "GB/s",
            "h2d_bytes_per_step": n, "d2h_bytes_per_step": int(4 * hr.n_struct + 128),
            "ms_per_step": round(e2e_s * 1e3, 3), "gpu_launches_per_step": e2e_launches,
-           "api": "pars_scan_host, pinned input: chunked copy-in, chunk scans and copy-out overlap"}
+           "api": "pars_scan_host, pinned input",
+           "transport": ("whole", "pipelined", "rerun")[hr.transport], "chunks": int(hr.chunks)}
 
     secondary = None
     if not args.no_secondary:
@@ -456,6 +457,22 @@ def main():
         jms, jscan, jpair, jl, jr = time_device(js, jt, max(5, args.steps), 3, stream, True,
                                                barrier)
         jalg = jd.size + 4 * jr.n_struct + 4 * jr.n_brackets + 4 * jr.n_struct
+        # the same document through pars_scan_host: pinned input, offsets and pairs home
+        jpin = torch.from_numpy(jd).pin_memory()
+        jhr = _lib.HostResult()
+        jflags = _lib.PARS_RUN_PAIRS | _lib.PARS_WANT_PAIRS
+
+        def jhost():
+            _lib.check(L.pars_scan_host(sc.ctx.handle, js.plan_id, ctypes.c_void_p(jpin.data_ptr()),
+                                        jd.size, jflags, ctypes.c_void_p(stream.cuda_stream),
+                                        ctypes.byref(jhr)), sc.ctx.handle)
+        for _ in range(3):
+            jhost()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            jhost()
+        je2e_s = (time.perf_counter() - t0) / 10
         secondary = {
             "workload": "json_64MiB_single_document", "bytes": int(jd.size),
             "GBps": round(jd.size / (jms / 1e3) / 1e9, 3), "ms_per_step": round(jms, 4),
@@ -464,6 +481,11 @@ def main():
             "roofline_pipeline_frac": round(jalg / (jms / 1e3) / 1e9 / peak, 4),
             "gpu_launches_per_step": jl / max(5, args.steps),
             "kernel_path": jr.kernel_path,
+            "e2e": {"value": round(jd.size / je2e_s / 1e9, 3), "unit": "GB/s",
+                    "ms_per_step": round(je2e_s * 1e3, 4), "h2d_bytes_per_step": int(jd.size),
+                    "d2h_bytes_per_step": int(8 * jhr.n_struct + 128),
+                    "transport": ("whole", "pipelined", "rerun")[jhr.transport],
+                    "chunks": int(jhr.chunks)},
         }
         del jt
 

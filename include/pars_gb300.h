@@ -105,7 +105,16 @@ typedef struct pars_host_result {     /* cf. host_result, pipeline.cuh:730-735 *
   const int32_t* pair_pos;
   uint64_t n_struct;
   int32_t balanced, well_formed, max_depth, unclosed_mode;
+  /* how the document crossed: PARS_TRANSPORT_WHOLE (one copy, then the scan),
+   * PARS_TRANSPORT_PIPELINED (pinned input in `chunks` chunks whose copy-in, scan and
+   * copy-out overlap) or PARS_TRANSPORT_RERUN (pipelined, then rerun whole because
+   * the reserved outputs overflowed or the escape speculation failed) */
+  int32_t transport, chunks;
 } pars_host_result;
+
+#define PARS_TRANSPORT_WHOLE 0
+#define PARS_TRANSPORT_PIPELINED 1
+#define PARS_TRANSPORT_RERUN 2
 
 /* Carry between chunks of one document (cf. chunk_carry, pipeline.cuh:737-743).
  * Opaque to the caller; zero-initialise it for the first chunk. */

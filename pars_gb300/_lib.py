@@ -49,7 +49,11 @@ class HostResult(ctypes.Structure):
         ("pair_pos", ctypes.c_void_p), ("n_struct", ctypes.c_uint64),
         ("balanced", ctypes.c_int32), ("well_formed", ctypes.c_int32),
         ("max_depth", ctypes.c_int32), ("unclosed_mode", ctypes.c_int32),
+        ("transport", ctypes.c_int32), ("chunks", ctypes.c_int32),
     ]
+
+
+PARS_TRANSPORT_WHOLE, PARS_TRANSPORT_PIPELINED, PARS_TRANSPORT_RERUN = 0, 1, 2
 
 
 class ChunkCarry(ctypes.Structure):

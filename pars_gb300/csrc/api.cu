@@ -826,8 +826,8 @@ int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, u
 }
 
 // Pinned host copies of the outputs, grown to `need` entries; the first `keep`
-// structural offsets (and chars) already copied home move to the new buffers.
-int grow_host_out(pars_ctx* ctx, size_t need, size_t keep, bool chars) {
+// structural offsets (and chars, pairs) already copied home move to the new buffers.
+int grow_host_out(pars_ctx* ctx, size_t need, size_t keep, bool chars, bool pairs) {
 	if (need <= ctx->h_out_cap)
 		return 0;
 	const size_t cap = need + need / 2 + 1024;
@@ -841,6 +841,8 @@ int grow_host_out(pars_ctx* ctx, size_t need, size_t keep, bool chars) {
 		std::memcpy(pos, ctx->h_pos, keep * 4);
 		if (chars)
 			std::memcpy(chr, ctx->h_chars, keep);
+		if (pairs)
+			std::memcpy(pr, ctx->h_pair, keep * 4);
 	}
 	if (ctx->h_pos) cudaFreeHost(ctx->h_pos);
 	if (ctx->h_chars) cudaFreeHost(ctx->h_chars);
@@ -852,9 +854,11 @@ int grow_host_out(pars_ctx* ctx, size_t need, size_t keep, bool chars) {
 	return 0;
 }
 
+// Chunks of at least 16 MiB: below that the host's per-chunk submission (tensor map,
+// cooperative launch, carry read-back) outlasts the chunk's copy on fast scans.
 constexpr int	   kPipeChunks	   = 32;
-constexpr uint64_t kPipeMinChunk   = 4ull << 20;
-constexpr uint64_t kPipeMinBytes   = 8ull << 20;
+constexpr uint64_t kPipeMinChunk   = 16ull << 20;
+constexpr uint64_t kPipeMinBytes   = 2 * kPipeMinChunk;
 
 int pipe_setup(pars_ctx* ctx) {
 	auto& P = ctx->pipe;
@@ -878,11 +882,10 @@ int pipe_setup(pars_ctx* ctx) {
 	return 0;
 }
 
-// Whether a pinned host document takes the pipelined path: a bracket-aware or
-// bracket-less fast path (the escape path may need a whole-document rescan under
-// exact descriptor semantics), no per-byte bitmap, no stage timing.
+// Whether a pinned host document takes the pipelined path: a warp-specialised fast
+// path, no per-byte bitmap, no stage timing.
 bool pipe_applies(const pars_ctx* ctx, const Plan* pl, uint64_t n, uint32_t flags) {
-	return n >= kPipeMinBytes && n < (1ull << 32) && !ctx->profiling && use_ws(pl->path) && pl->path != kPathEscape
+	return n >= kPipeMinBytes && n < (1ull << 32) && !ctx->profiling && use_ws(pl->path)
 		&& !(flags & (PARS_WANT_MASK | PARS_FORCE_GENERIC));
 }
 
@@ -892,8 +895,10 @@ bool pipe_applies(const pars_ctx* ctx, const Plan* pl, uint64_t n, uint32_t flag
 // i-1 exactly like pars_scan_chunk; once chunk i's scan has finished the host reads
 // its running structural count and sends that chunk's offsets (and chars) home on a
 // copy-out stream while later chunks are still crossing.  R6 runs after the last
-// chunk; pair_pos follows it.  `*redo` = outputs overflowed the reserved capacity:
-// the document is resident and the caller reruns it on the whole-document path.
+// chunk; pair_pos follows it.  `*redo` = outputs overflowed the reserved capacity,
+// or the escape path's speculation failed (a quote escaped outside a string): the
+// document is resident and the caller reruns it on the whole-document path, which
+// grows the outputs or switches to exact descriptor semantics.
 int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n, uint32_t flags,
 						cudaStream_t st, pars_host_result* out, bool* redo) {
 	*redo = false;
@@ -902,9 +907,12 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 	auto&		   P		 = ctx->pipe;
 	const bool	   run_pairs = (flags & PARS_RUN_PAIRS) && pl->host.has_brackets;
 	const bool	   chars	 = (flags & PARS_WANT_CHARS) != 0;
+	// without R6 the scan's pair_pos (-1 everywhere) is final chunk by chunk
+	const bool	   pairs_early = (flags & PARS_WANT_PAIRS) && !run_pairs;
 	const uint64_t align	 = 64ull << 10;
 	const uint64_t chunk	 = std::max(kPipeMinChunk, ((n + kPipeChunks - 1) / kPipeChunks + align - 1) / align * align);
-	const int	   nch		 = static_cast<int>((n + chunk - 1) / chunk);
+	// the last chunk takes the remainder rather than leaving a short one behind
+	const int	   nch		 = static_cast<int>(std::max<uint64_t>(1, n / chunk));
 	const uint64_t want_s	 = std::max<uint64_t>(ctx->cap_s, n / 3 + 4096);
 	const uint64_t want_b	 = std::max<uint64_t>(ctx->cap_b, pl->host.has_brackets ? n / 6 + 4096 : 1024);
 	if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
@@ -914,8 +922,9 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 	CK(cudaEventRecord(P.start, st));
 	CK(cudaStreamWaitEvent(P.in_st, P.start, 0));
 	CK(cudaStreamWaitEvent(P.out_st, P.start, 0));
+	auto chunk_len = [&](int i) { return i == nch - 1 ? n - i * chunk : chunk; };
 	for (int i = 0; i < nch; ++i) {
-		const uint64_t off = i * chunk, len = std::min(chunk, n - off);
+		const uint64_t off = i * chunk, len = chunk_len(i);
 		CK(cudaMemcpyAsync(d + off, h_in + off, len, cudaMemcpyHostToDevice, P.in_st));
 		CK(cudaEventRecord(P.in_ev[i], P.in_st));
 	}
@@ -924,7 +933,7 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 	ctx->cur_in = nullptr;	// the chunk scans write the bracket bytes themselves
 	const uint32_t sflags = (flags & (PARS_WANT_PAIRS | PARS_WANT_CHARS)) | kScanOwnBchar;
 	for (int i = 0; i < nch; ++i) {
-		const uint64_t off = i * chunk, len = std::min(chunk, n - off);
+		const uint64_t off = i * chunk, len = chunk_len(i);
 		DevCarry*	   cin	= ctx->carry + (i & 1);
 		DevCarry*	   cout = ctx->carry + ((i + 1) & 1);
 		CK(cudaStreamWaitEvent(st, P.in_ev[i], 0));
@@ -950,10 +959,10 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 		}
 		if (ns > ctx->h_out_cap) {
 			// size the host copies for the whole document from the density so far
-			const uint64_t covered = std::min(n, (i + 1) * chunk);
+			const uint64_t covered = i == nch - 1 ? n : (i + 1) * chunk;
 			const uint64_t est	   = static_cast<uint64_t>(static_cast<double>(ns) / covered * n * 1.05);
 			CK(cudaStreamSynchronize(P.out_st));
-			if (int r = grow_host_out(ctx, std::max(ns, est), prev, chars))
+			if (int r = grow_host_out(ctx, std::max(ns, est), prev, chars, pairs_early))
 				return r;
 		}
 		if (ns > prev) {
@@ -962,6 +971,9 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 			if (chars)
 				CK(cudaMemcpyAsync(ctx->h_chars + prev, static_cast<const uint8_t*>(ctx->chars.p) + prev,
 								   ns - prev, cudaMemcpyDeviceToHost, P.out_st));
+			if (pairs_early)
+				CK(cudaMemcpyAsync(ctx->h_pair + prev, static_cast<const int32_t*>(ctx->pair.p) + prev,
+								   (ns - prev) * 4, cudaMemcpyDeviceToHost, P.out_st));
 		}
 		prev = ns;
 	}
@@ -972,7 +984,7 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 		reset_after_error(ctx, st);
 		return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
 	}
-	if (over || r.n_struct > ctx->cap_s || r.n_brackets > ctx->cap_b) {
+	if (over || r.n_struct > ctx->cap_s || r.n_brackets > ctx->cap_b || r.spec_fail) {
 		*redo = true;
 		return 0;
 	}
@@ -987,9 +999,9 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 			return fail(ctx, PARS_ETIMEDOUT, "a bounded device wait gave up");
 		}
 	}
-	if (int e = grow_host_out(ctx, r.n_struct, prev, chars))
+	if (int e = grow_host_out(ctx, r.n_struct, prev, chars, pairs_early))
 		return e;
-	if ((flags & PARS_WANT_PAIRS) && r.n_struct) {
+	if ((flags & PARS_WANT_PAIRS) && !pairs_early && r.n_struct) {
 		CK(cudaMemcpyAsync(ctx->h_pair, ctx->pair.p, r.n_struct * 4, cudaMemcpyDeviceToHost, st));
 		CK(cudaStreamSynchronize(st));
 	}
@@ -1003,6 +1015,8 @@ int scan_host_pipelined(pars_ctx* ctx, Plan* pl, const uint8_t* h_in, uint64_t n
 	out->well_formed   = dr.well_formed;
 	out->max_depth	   = dr.max_depth;
 	out->unclosed_mode = dr.unclosed_mode;
+	out->transport	   = PARS_TRANSPORT_PIPELINED;
+	out->chunks		   = nch;
 	return 0;
 }
 
@@ -1185,7 +1199,7 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 			return r;
 		if (!redo)
 			return 0;
-		resident = true;  // outputs overflowed: rerun the resident document below
+		resident = true;  // rerun the resident document below
 	}
 	if (n && !resident) {
 		if (pinned) {
@@ -1211,7 +1225,7 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 	if (int r = scan_device_impl(ctx, pl, static_cast<const uint8_t*>(ctx->d_in.p), n, flags, st, &dr))
 		return r;
 	const size_t need = dr.n_struct;
-	if (int r = grow_host_out(ctx, need, 0, false))
+	if (int r = grow_host_out(ctx, need, 0, false, false))
 		return r;
 	if (need) {
 		CK(cudaMemcpyAsync(ctx->h_pos, dr.structural, need * 4, cudaMemcpyDeviceToHost, st));
@@ -1229,6 +1243,8 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 	out->well_formed   = dr.well_formed;
 	out->max_depth	   = dr.max_depth;
 	out->unclosed_mode = dr.unclosed_mode;
+	out->transport	   = resident ? PARS_TRANSPORT_RERUN : PARS_TRANSPORT_WHOLE;
+	out->chunks		   = 1;
 	return 0;
 }
 

@@ -123,6 +123,8 @@ class HostResult:
     well_formed: bool
     max_depth: int
     unclosed_mode: bool
+    transport: str = "whole"   # "whole", "pipelined" or "rerun"
+    chunks: int = 1
 
 
 class Context:
@@ -228,10 +230,10 @@ class Scanner:
         return self.scan_device(t.data_ptr(), t.numel(), stream=stream, **kw)
 
     def scan_host(self, data, stream: int = 0, want_pairs: bool = False,
-                  want_chars: bool = False) -> HostResult:
+                  want_chars: bool = False, run_pairs: bool = True) -> HostResult:
         a = np.ascontiguousarray(np.frombuffer(memoryview(data), np.uint8)
                                  if not isinstance(data, np.ndarray) else data, dtype=np.uint8)
-        flags = PARS_RUN_PAIRS | (PARS_WANT_PAIRS if want_pairs else 0) | (
+        flags = (PARS_RUN_PAIRS if run_pairs else 0) | (PARS_WANT_PAIRS if want_pairs else 0) | (
             PARS_WANT_CHARS if want_chars else 0)
         r = _lib.HostResult()
         ptr = a.ctypes.data if a.size else None
@@ -248,7 +250,8 @@ class Scanner:
                           host(r.pair_pos, ctypes.c_int32, np.int32),
                           host(r.chars, ctypes.c_uint8, np.uint8),
                           bool(r.balanced), bool(r.well_formed), int(r.max_depth),
-                          bool(r.unclosed_mode))
+                          bool(r.unclosed_mode),
+                          ("whole", "pipelined", "rerun")[r.transport], int(r.chunks))
 
     # ---- chunked stage 1 -----------------------------------------------------------
     def reserve_struct(self, cap: int) -> None:

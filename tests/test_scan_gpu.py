@@ -198,13 +198,13 @@ def test_scan_host_matches_device(scanners):
 
 @pytest.mark.parametrize("grammar", GRAMMARS)
 def test_scan_host_pipelined(grammar):
-    """Pinned input of 20 MiB + 5 bytes (five 4 MiB chunks and a ragged end) through
-    pars_scan_host, which pipelines copy-in, chunk scans and copy-out on the fast
-    paths: offsets, chars, pairs and flags against the oracle.  A fresh context, so
+    """Pinned input of 40 MiB + 5 bytes (a 16 MiB chunk and a ragged 24 MiB one)
+    through pars_scan_host, which pipelines copy-in, chunk scans and copy-out on the
+    fast paths: offsets, chars, pairs and flags against the oracle.  A fresh context, so
     the host copies grow while the document is in flight."""
     from tests_alphabets import ALPHABETS
     plan = plan_bytes(grammar)
-    data = synth.alpha(4099, ALPHABETS[grammar], (20 << 20) + 5)
+    data = synth.alpha(4099, ALPHABETS[grammar], (40 << 20) + 5)
     pinned = torch.from_numpy(data).pin_memory()
     e = expected_from_oracle(plan, data)
     sc = Scanner(plan, ctx=Context(0))
@@ -214,18 +214,74 @@ def test_scan_host_pipelined(grammar):
         assert np.array_equal(h.chars, e["chars"])
         assert np.array_equal(h.pair_pos, e["pair"])
         assert (h.unclosed_mode, h.balanced, h.well_formed, h.max_depth) == e["meta"]
+        # fast paths pipeline (random alphabets may overflow or fail the escape
+        # speculation and rerun); the general path copies the whole document first
+        assert h.transport == ("whole" if sc.path == "generic" else h.transport)
+        assert (h.transport == "whole") == (sc.path == "generic")
+
+
+def json_runs_across(n: int, step: int = 64 << 10) -> np.ndarray:
+    """A JSON array of strings whose backslash runs straddle every multiple of `step`
+    bytes (every place a pipelined chunk can end), 0-6 backslashes before the cut,
+    odd runs escaping a quote inside the string, even runs ending it."""
+    out = bytearray(b"[")
+    k = 1
+    while k * step < n - 256:
+        cut = k * step
+        j = k % 7                 # backslashes before the cut
+        run = j + 1 + k % 5       # run length: crosses the cut
+        while cut - j - len(out) - 1 > 200:
+            out += b'"' + b"x" * 90 + b'",'
+        pad = cut - j - len(out) - 1
+        if pad >= 0:
+            out += b'"' + b"a" * pad + b"\\" * run + (b'"' if run % 2 == 0 else b'"z"') + b","
+        k += 1
+    out += b"0]"
+    return np.frombuffer(bytes(out), np.uint8).copy()
+
+
+@pytest.mark.parametrize("doc", ["synthetic", "runs_across_cuts"])
+def test_scan_host_pipelined_json(scanners, doc):
+    """JSON on the pipelined escape path: chunk carries hold the pending escape and the
+    in-string state; a document with no quote escaped outside a string completes
+    without a rerun, bit-exact against the oracle."""
+    plan = plan_bytes("json")
+    data = synth.json_doc(23, 72 << 20) if doc == "synthetic" else json_runs_across(40 << 20)
+    pinned = torch.from_numpy(data).pin_memory()
+    e = expected_from_oracle(plan, data)
+    h = scanners["json"].scan_host(pinned.numpy(), want_pairs=True, want_chars=True)
+    assert (h.transport, h.chunks > 1) == ("pipelined", True)
+    assert np.array_equal(h.structural, e["pos"])
+    assert np.array_equal(h.chars, e["chars"])
+    assert np.array_equal(h.pair_pos, e["pair"])
+    assert (h.unclosed_mode, h.balanced, h.well_formed, h.max_depth) == e["meta"]
+
+
+def test_scan_host_pipelined_no_r6():
+    """want_pairs without R6: pair_pos is -1 at every structural and travels home
+    chunk by chunk with the offsets; the validity flags keep their defaults."""
+    plan = plan_bytes("json")
+    data = synth.json_doc(29, 40 << 20)
+    pinned = torch.from_numpy(data).pin_memory()
+    e = expected_from_oracle(plan, data)
+    h = Scanner(plan).scan_host(pinned.numpy(), want_pairs=True, run_pairs=False)
+    assert h.transport == "pipelined"
+    assert np.array_equal(h.structural, e["pos"])
+    assert h.pair_pos.size == e["pos"].size and np.all(h.pair_pos == -1)
+    assert (h.balanced, h.well_formed, h.max_depth) == (True, True, 0)
 
 
 def test_scan_host_pipelined_overflow():
     """A CSV document of delimiters only has a structural at every byte, more than the
     pipelined path reserves: it reruns the resident document on the whole-document
     path and still returns every offset."""
-    n = (12 << 20) + 3
+    n = (36 << 20) + 3
     data = np.full(n, ord(","), np.uint8)
     data[::7] = ord("a")
     pinned = torch.from_numpy(data).pin_memory()
     sc = Scanner(plan_bytes("csv"), ctx=Context(0))
     h = sc.scan_host(pinned.numpy(), want_chars=True)
+    assert h.transport == "rerun"
     pos = np.nonzero(data == ord(","))[0].astype(np.uint32)
     assert np.array_equal(h.structural, pos)
     assert np.all(h.chars == ord(","))
