@@ -286,22 +286,27 @@ int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_t* d_in, ui
                              void* stream);
 
 /* ---- autotuning ------------------------------------------------------------ */
-/* No counterpart in the reference.  The scan's launch parameter is the persistent
- * grid size G, which is also its look-back depth (each tile folds the G - 1 tiles
- * since its CTA's previous tile).  pars_autotune times the resident grid and 3/4,
- * 2/3 and 1/2 of it on a sample document (device memory) and keeps the fastest for
- * the plan's scan path and the sample's size bucket (floor(log2(n))); later scans
- * of that path and bucket use it.  Results never depend on the grid.
- * pars_tune_set sets the grid of a path and size bucket directly (0 = default). */
+/* No counterpart in the reference.  The scan's launch parameters are the tile
+ * shape (16 worker warps on 32 KiB tiles, 544 threads per block, or 24 on 48 KiB
+ * tiles, 800 threads) and the persistent grid size G, which is also the look-back
+ * depth (each tile folds the G - 1 tiles since its CTA's previous tile).
+ * pars_autotune times, for each shape, the resident grid and 3/4, 2/3 and 1/2 of it
+ * on a sample document (device memory) and keeps the fastest pair for the plan's
+ * scan path and the sample's size bucket (floor(log2(n))); later single-document
+ * scans of that path and bucket use it.  Results never depend on either.
+ * pars_tune_set sets them directly (grid 0 = the resident grid; workers 0 = by
+ * size: 24 from 1 MiB up, else 16). */
 typedef struct pars_tune_report {
   uint32_t path, bucket, grid, n_candidates;
   uint32_t cand_grid[8];
   float cand_ms[8];
+  uint32_t workers;          /* worker warps of the chosen tile shape (0: general path) */
+  uint32_t cand_workers[8];
 } pars_tune_report;
 
 int pars_autotune(pars_ctx* ctx, int plan_id, const uint8_t* d_sample, uint64_t n,
                   uint32_t flags, void* stream, pars_tune_report* out);
-int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid);
+int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid, uint32_t workers);
 
 /* ---- profiling ------------------------------------------------------------ */
 /* cf. stage_times (pipeline.cuh:746-748, 767-774, 998-1011): when enabled, the

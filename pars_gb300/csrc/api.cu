@@ -33,16 +33,17 @@ namespace pars {
 int		   scan_smem_bytes(int path);
 const void* scan_kernel(int path);
 int		   scan_ws_max_grid();
-int		   scan_ws_threads();
-int		   scan_ws_tile_bytes();
+int		   scan_ws_threads(int shape);
+int		   scan_ws_tile_bytes(int shape);
+int		   scan_ws_box_rows(int shape);
 struct WsArgs {
 	ScanArgs		   a;
 	unsigned long long rows_full;
 	BatchDesc		   bd;
 };
 const void* scan_ws_batch_kernel(int path, bool brackets);
-int		   scan_ws_smem_bytes();
-const void* scan_ws_kernel(int path, bool brackets);
+int		   scan_ws_smem_bytes(int shape);
+const void* scan_ws_kernel(int path, bool brackets, int shape);
 int		   sort_tile_keys();
 const void* bchar_gather_kernel();
 struct SortPass;
@@ -95,10 +96,12 @@ struct pars_ctx {
 	uint64_t		   arena_used  = 0;
 	int				   num_sms	   = 0;
 	int				   scan_blocks[5] = {0, 0, 0, 0, 0};
-	int				   fast_blocks[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	int				   fast_blocks[kWsShapes][10] = {};
 	uint64_t		   gen = 0;	 // bumped whenever a device buffer moves
-	// grid sizes chosen by pars_autotune / pars_tune_set: [path][log2 size bucket], 0 = default
+	// grid sizes and tile shapes chosen by pars_autotune / pars_tune_set:
+	// [path][log2 size bucket]; grid 0 = the resident grid, shape 0 = by size
 	int				   tuned_grid[5][48] = {};
+	int				   tuned_shape[5][48] = {};	// tile shape + 1
 	std::string		   err;
 	std::vector<Plan*> plans;
 	unsigned int	   epoch = 0;
@@ -397,33 +400,34 @@ bool use_ws(int path) {
 	return path == kPathNone || path == kPathParity || path == kPathDoubled || path == kPathEscape;
 }
 
-const void* fast_kernel(int path, bool br) {
-	return use_ws(path) ? scan_ws_kernel(path, br) : nullptr;
+const void* fast_kernel(int path, bool br, int shape) {
+	return use_ws(path) ? scan_ws_kernel(path, br, shape) : nullptr;
 }
 
-int fast_threads(int path) {
-	return use_ws(path) ? scan_ws_threads() : kScanThreads;
+int fast_threads(int path, int shape) {
+	return use_ws(path) ? scan_ws_threads(shape) : kScanThreads;
 }
 
-int fast_smem(int path) {
-	return use_ws(path) ? scan_ws_smem_bytes() : 0;
+int fast_smem(int path, int shape) {
+	return use_ws(path) ? scan_ws_smem_bytes(shape) : 0;
 }
 
-int ensure_fast_config(pars_ctx* ctx, int path, bool br) {
+int ensure_fast_config(pars_ctx* ctx, int path, bool br, int shape) {
 	const int slot = path * 2 + (br ? 1 : 0);
-	if (ctx->fast_blocks[slot])
+	if (ctx->fast_blocks[shape][slot])
 		return 0;
-	const void* k	 = fast_kernel(path, br);
-	const int	smem = fast_smem(path);
+	const void* k	 = fast_kernel(path, br, shape);
+	const int	smem = fast_smem(path, shape);
 	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 	int per_sm = 0;
-	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, fast_threads(path), smem));
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, fast_threads(path, shape), smem));
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "fast scan kernel does not fit on an SM");
 	// the look-back window of a tile spans one wave (G tiles), held by one warp
-	ctx->fast_blocks[slot] = std::min(per_sm * ctx->num_sms, scan_ws_max_grid());
+	ctx->fast_blocks[shape][slot] = std::min(per_sm * ctx->num_sms, scan_ws_max_grid());
 	return 0;
 }
+
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -442,9 +446,9 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 	return fn;
 }
 
-// The document as a [rows][128] byte tensor (full rows only), 256-row boxes,
-// 128-byte swizzle.
-int make_row_map(pars_ctx* ctx, const uint8_t* base, uint64_t rows, CUtensorMap* map) {
+// The document as a [rows][128] byte tensor (full rows only), boxes of a tile's
+// rows (or half of them) for tile shape `shape`, 128-byte swizzle.
+int make_row_map(pars_ctx* ctx, const uint8_t* base, uint64_t rows, CUtensorMap* map, int shape) {
 	std::memset(map, 0, sizeof *map);
 	if (rows == 0)
 		return 0;
@@ -453,7 +457,7 @@ int make_row_map(pars_ctx* ctx, const uint8_t* base, uint64_t rows, CUtensorMap*
 		return fail(ctx, PARS_ECUDA, "cuTensorMapEncodeTiled unavailable");
 	const cuuint64_t dims[2]	= {128, rows};
 	const cuuint64_t strides[1] = {128};
-	const cuuint32_t box[2]		= {128, 256};
+	const cuuint32_t box[2]		= {128, static_cast<cuuint32_t>(scan_ws_box_rows(shape))};
 	const cuuint32_t estr[2]	= {1, 1};
 	const CUresult	 r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(base), dims,
 							 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -476,13 +480,24 @@ int size_bucket(uint64_t n) {
 	return b;
 }
 
+// Tile shape of a single-document scan: the tuned one, else 24 workers (48 KiB
+// tiles) from 1 MiB up, where more resident warps hide more latency, and 16
+// workers (32 KiB tiles) below, where a tile pass is most of the work.
+int ws_shape(const pars_ctx* ctx, int path, uint64_t n) {
+	const int t = ctx->tuned_shape[path][size_bucket(n)];
+	if (t > 0)
+		return t - 1;
+	return n >= (1ull << 20) ? 1 : 0;
+}
+
 // `first` = first launch of a document: clears the result block + key histogram.
 int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true) {
 	const uint64_t o	 = reinterpret_cast<uintptr_t>(s.d_in) & 15u;
 	const uint8_t* base	 = s.d_in - o;
 	const uint64_t total = o + s.n;
 	const bool	   fast	 = s.path != kPathGeneric;
-	const uint64_t tile	 = (fast && use_ws(s.path)) ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;
+	const int	   shape = (fast && use_ws(s.path)) ? ws_shape(ctx, s.path, s.n) : 0;
+	const uint64_t tile	 = (fast && use_ws(s.path)) ? static_cast<uint64_t>(scan_ws_tile_bytes(shape)) : kTileBytes;
 	const uint64_t ntiles = (total + tile - 1) / tile;
 	// fast kernels: AGG and INCL words, three 64-bit planes each
 	const size_t tdesc = fast ? 6 * sizeof(uint64_t) : sizeof(TileDescG);
@@ -493,7 +508,7 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	// in the plan its bracket planes are empty).
 	const bool br_kernel = pl->host.has_brackets != 0 || (use_ws(s.path) && (s.flags & PARS_WANT_MASK));
 	if (fast) {
-		if (int r = ensure_fast_config(ctx, s.path, br_kernel))
+		if (int r = ensure_fast_config(ctx, s.path, br_kernel, shape))
 			return r;
 	} else {
 		if (int r = ensure_scan_config(ctx, s.path))
@@ -529,23 +544,18 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 	void* args[] = {&a};
 	if (fast && use_ws(s.path)) {
 		const bool	br	 = br_kernel;
-		int			g	 = ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)];
+		int			g	 = ctx->fast_blocks[shape][s.path * 2 + (br ? 1 : 0)];
 		const int	tg	 = ctx->tuned_grid[s.path][size_bucket(s.n)];
 		if (tg > 0 && tg < g)
 			g = tg;
 		const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, static_cast<uint64_t>(g)));
 		WsArgs		wa {a, total / 128};
 		CUtensorMap map;
-		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+		if (int r = make_row_map(ctx, base, wa.rows_full, &map, shape))
 			return r;
 		void* wargs[] = {&wa, &map};
-		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br), dim3(grid), dim3(fast_threads(s.path)),
-									   wargs, fast_smem(s.path), s.st));
-	} else if (fast) {
-		const bool br	= pl->host.has_brackets != 0;
-		const int  grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[s.path * 2 + (br ? 1 : 0)]));
-		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br), dim3(grid), dim3(fast_threads(s.path)),
-									   args, fast_smem(s.path), s.st));
+		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br, shape), dim3(grid), dim3(fast_threads(s.path, shape)),
+									   wargs, fast_smem(s.path, shape), s.st));
 	} else {
 		const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
 		CK(cudaLaunchCooperativeKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,
@@ -1402,14 +1412,15 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 	const bool	   ws	  = use_ws(pl->path) && pl->path != kPathEscape;
 	const int	   path	  = ws ? pl->path : kPathGeneric;
 	const bool	   br	  = pl->host.has_brackets != 0;
-	const uint64_t tile	  = ws ? static_cast<uint64_t>(scan_ws_tile_bytes()) : kTileBytes;
+	const int	   shape  = ws ? ws_shape(ctx, path, n) : 0;
+	const uint64_t tile	  = ws ? static_cast<uint64_t>(scan_ws_tile_bytes(shape)) : kTileBytes;
 	const uint64_t ntiles = (total + tile - 1) / tile;
 	const uint64_t desc	  = ntiles * (ws ? 3 * sizeof(uint64_t) : sizeof(TileDescG));
 	// what must start at zero: the result block, the counters, the descriptors in use
 	CK(cudaMemsetAsync(scr, 0, kNoAllocRbBytes + kNoAllocCtrBytes + desc, st));
 	if (n) {
 		if (ws) {
-			if (int r = ensure_fast_config(ctx, path, br))
+			if (int r = ensure_fast_config(ctx, path, br, shape))
 				return r;
 		} else if (int r = ensure_scan_config(ctx, path)) {
 			return r;
@@ -1431,14 +1442,14 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 		a.epoch	   = next_epoch(ctx);
 		a.flags	   = 0;
 		if (ws) {
-			const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[path * 2 + (br ? 1 : 0)]));
+			const int	grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->fast_blocks[shape][path * 2 + (br ? 1 : 0)]));
 			WsArgs		wa {a, total / 128};
 			CUtensorMap map;
-			if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+			if (int r = make_row_map(ctx, base, wa.rows_full, &map, shape))
 				return r;
 			void* wargs[] = {&wa, &map};
-			CK(cudaLaunchCooperativeKernel(fast_kernel(path, br), dim3(grid), dim3(fast_threads(path)), wargs,
-										   fast_smem(path), st));
+			CK(cudaLaunchCooperativeKernel(fast_kernel(path, br, shape), dim3(grid), dim3(fast_threads(path, shape)),
+										   wargs, fast_smem(path, shape), st));
 		} else {
 			const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[path]));
 			void*	  args[] = {&a};
@@ -1472,10 +1483,10 @@ int ensure_batch_config(pars_ctx* ctx, int path, bool br) {
 	if (ctx->batch.blocks[slot])
 		return 0;
 	const void* k	 = scan_ws_batch_kernel(path, br);
-	const int	smem = scan_ws_smem_bytes();
+	const int	smem = scan_ws_smem_bytes(0);
 	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 	int per_sm = 0;
-	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, scan_ws_threads(), smem));
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, scan_ws_threads(0), smem));
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "batch scan kernel does not fit on an SM");
 	ctx->batch.blocks[slot] = std::min(per_sm * ctx->num_sms, 1024);
@@ -1643,7 +1654,8 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 	std::vector<uint32_t> item_begin(G + 1), doc_cta(ndocs);
 	std::vector<uint64_t> region_s(G + 1), region_b(G + 1);
 	for (uint32_t d = 0; d <= ndocs; ++d) doc_start[d] = o + offsets[d];
-	items.reserve(ndocs + total / 32768 + 16);
+	const uint64_t tile_b = static_cast<uint64_t>(scan_ws_tile_bytes(0));  // the batch kernel's shape
+	items.reserve(ndocs + total / tile_b + 16);
 	for (int b = 0; b < G; ++b) {
 		item_begin[b] = static_cast<uint32_t>(items.size());
 		for (uint32_t d : cta_docs[b]) {
@@ -1651,7 +1663,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			const uint64_t lo = doc_start[d], hi = doc_start[d + 1];
 			if (hi == lo)
 				continue;
-			const uint64_t nt = (hi - (lo & ~uint64_t(127)) + 32767) / 32768;
+			const uint64_t nt = (hi - (lo & ~uint64_t(127)) + tile_b - 1) / tile_b;
 			for (uint64_t j = 0; j < nt; ++j) items.push_back((static_cast<uint64_t>(d) << 32) | j);
 		}
 		region_s[b + 1] = region_s[b] + load[b] / 2 + 4096;
@@ -1751,7 +1763,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			a.flags |= PARS_WANT_PAIRS;	 // R6 overwrites the brackets' entries
 		WsArgs		wa {a, total / 128, bd};
 		CUtensorMap map;
-		if (int r = make_row_map(ctx, base, wa.rows_full, &map))
+		if (int r = make_row_map(ctx, base, wa.rows_full, &map, 0))
 			return r;
 		void*	 wargs[] = {&wa, &map};
 		uint64_t nl		 = 0;  // kernels of the sequence
@@ -1766,8 +1778,8 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		CK(cudaMemsetAsync(B.cta_bcount.p, 0, static_cast<size_t>(G) * 4, st));
 		CK(cudaMemsetAsync(B.bres, 0, sizeof(DevResult), st));
 		CK(cudaMemsetAsync(ctx->rb, 0, sizeof(ResBlock), st));
-		CK(cudaLaunchKernel(scan_ws_batch_kernel(path, br), dim3(G), dim3(scan_ws_threads()), wargs,
-							scan_ws_smem_bytes(), st));
+		CK(cudaLaunchKernel(scan_ws_batch_kernel(path, br), dim3(G), dim3(scan_ws_threads(0)), wargs,
+							scan_ws_smem_bytes(0), st));
 		nl++;
 		if (br) {
 			BatchR6 r6 {};
@@ -1987,13 +1999,20 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 // ================================================================================
 // Autotuning
 // ================================================================================
-extern "C" int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid) {
+extern "C" int pars_tune_set(pars_ctx* ctx, int plan_id, uint64_t n, uint32_t grid, uint32_t workers) {
 	Plan* pl = get_plan(ctx, plan_id);
 	if (!pl)
 		return ctx ? fail(ctx, PARS_EINVAL, "bad plan id") : PARS_EINVAL;
 	if (pl->path < 0 || pl->path > 4)
 		return fail(ctx, PARS_EINVAL, "bad path");
-	ctx->tuned_grid[pl->path][size_bucket(n)] = static_cast<int>(grid);
+	int shape = -1;
+	for (int t = 0; t < kWsShapes; ++t)
+		if (workers == static_cast<uint32_t>(kWsShapeWorkers[t]))
+			shape = t;
+	if (workers && shape < 0)
+		return fail(ctx, PARS_EINVAL, "workers must be 0, 16 or 24");
+	ctx->tuned_grid[pl->path][size_bucket(n)]  = static_cast<int>(grid);
+	ctx->tuned_shape[pl->path][size_bucket(n)] = workers ? shape + 1 : 0;
 	return 0;
 }
 
@@ -2014,55 +2033,79 @@ extern "C" int pars_autotune(pars_ctx* ctx, int plan_id, const uint8_t* d_sample
 		return 0;
 	}
 	const bool br = pl->host.has_brackets != 0;
-	if (int r = ensure_fast_config(ctx, path, br))
-		return r;
-	const int full = ctx->fast_blocks[path * 2 + (br ? 1 : 0)];
-	// candidates: the whole resident grid and fractions of it (look-back window G - 1)
-	int cands[8], nc = 0;
-	for (int div : {4, 3, 2}) {
-		const int g = full * (div - 1) / div;
-		if (g >= 1)
-			cands[nc++] = g;
+	// candidates: each tile shape (worker count) with its whole resident grid and
+	// fractions of it (the look-back window is G - 1 tiles)
+	int cand_g[8], cand_s[8], nc = 0;
+	for (int shape = 0; shape < kWsShapes; ++shape) {
+		if (int r = ensure_fast_config(ctx, path, br, shape))
+			return r;
+		const int full = ctx->fast_blocks[shape][path * 2 + (br ? 1 : 0)];
+		for (int div : {4, 3, 2}) {
+			const int g = full * (div - 1) / div;
+			if (g >= 1 && nc < 7) {
+				cand_g[nc]	 = g;
+				cand_s[nc++] = shape;
+			}
+		}
+		cand_g[nc]	 = full;
+		cand_s[nc++] = shape;
 	}
-	cands[nc++] = full;
 	cudaEvent_t e0, e1;
 	CK(cudaEventCreate(&e0));
 	CK(cudaEventCreate(&e1));
-	const int saved = ctx->tuned_grid[path][bucket];
-	float	  best	= 0;
-	int		  bestg = full;
+	const int saved_g = ctx->tuned_grid[path][bucket], saved_s = ctx->tuned_shape[path][bucket];
+	auto restore = [&] {
+		ctx->tuned_grid[path][bucket]  = saved_g;
+		ctx->tuned_shape[path][bucket] = saved_s;
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+	};
+	float best = 0;
+	int	  bi   = 0;
 	for (int i = 0; i < nc; ++i) {
-		ctx->tuned_grid[path][bucket] = cands[i];
+		ctx->tuned_grid[path][bucket]  = cand_g[i];
+		ctx->tuned_shape[path][bucket] = cand_s[i] + 1;
 		pars_device_result r {};
 		for (int w = 0; w < 2; ++w)
 			if (int e = scan_device_impl(ctx, pl, d_sample, n, flags, st, &r)) {
-				ctx->tuned_grid[path][bucket] = saved;
+				restore();
 				return e;
 			}
 		float ms = 1e30f;
 		for (int rep = 0; rep < 3; ++rep) {
-			CK(cudaEventRecord(e0, st));
-			if (int e = scan_device_impl(ctx, pl, d_sample, n, flags, st, &r)) {
-				ctx->tuned_grid[path][bucket] = saved;
-				return e;
-			}
-			CK(cudaEventRecord(e1, st));
-			CK(cudaEventSynchronize(e1));
+			cudaError_t ce = cudaEventRecord(e0, st);
+			if (ce == cudaSuccess)
+				if (int e = scan_device_impl(ctx, pl, d_sample, n, flags, st, &r)) {
+					restore();
+					return e;
+				}
+			if (ce == cudaSuccess)
+				ce = cudaEventRecord(e1, st);
+			if (ce == cudaSuccess)
+				ce = cudaEventSynchronize(e1);
 			float t = 0;
-			CK(cudaEventElapsedTime(&t, e0, e1));
+			if (ce == cudaSuccess)
+				ce = cudaEventElapsedTime(&t, e0, e1);
+			if (ce != cudaSuccess) {
+				restore();
+				return cuda_fail(ctx, ce, "autotune timing");
+			}
 			ms = std::min(ms, t);
 		}
-		out->cand_grid[i] = static_cast<uint32_t>(cands[i]);
-		out->cand_ms[i]	  = ms;
+		out->cand_grid[i]	 = static_cast<uint32_t>(cand_g[i]);
+		out->cand_workers[i] = static_cast<uint32_t>(kWsShapeWorkers[cand_s[i]]);
+		out->cand_ms[i]		 = ms;
 		if (i == 0 || ms < best) {
-			best  = ms;
-			bestg = cands[i];
+			best = ms;
+			bi	 = i;
 		}
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
-	out->n_candidates			  = static_cast<uint32_t>(nc);
-	out->grid					  = static_cast<uint32_t>(bestg);
-	ctx->tuned_grid[path][bucket] = bestg;
+	out->n_candidates			   = static_cast<uint32_t>(nc);
+	out->grid					   = static_cast<uint32_t>(cand_g[bi]);
+	out->workers				   = static_cast<uint32_t>(kWsShapeWorkers[cand_s[bi]]);
+	ctx->tuned_grid[path][bucket]  = cand_g[bi];
+	ctx->tuned_shape[path][bucket] = cand_s[bi] + 1;
 	return 0;
 }

@@ -35,6 +35,12 @@ constexpr std::uint32_t kClsDelim  = 1u << 24;
 // the bytes from the still-resident input.
 constexpr std::uint32_t kScanOwnBchar = 1u << 16;
 
+// Tile shapes of the warp-specialised scan: shape 0 runs 16 worker warps on 32 KiB
+// tiles, shape 1 runs 24 worker warps on 48 KiB tiles (single documents only; the
+// batch kernel uses shape 0).
+constexpr int kWsShapes			= 2;
+constexpr int kWsShapeWorkers[] = {16, 24};
+
 struct DevPlan {
 	std::uint32_t cls[256];			   // R1 classifier (classify.hpp:39-55) + fast-path delim
 	std::uint8_t  is_open[256];		   // nest.hpp:24-30

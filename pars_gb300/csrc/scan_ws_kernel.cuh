@@ -3,7 +3,8 @@
 // a quote automaton with a backslash escape (the JSON shape).
 //
 // Data movement.  The document is viewed as a 2-D tensor of 128-byte rows and
-// streamed in 32 KiB tiles (256 rows) by TMA tensor copies with the 128-byte
+// streamed in tiles of W x 2 KiB (W worker warps: 32 KiB = 256 rows for W = 16,
+// 48 KiB = two 192-row boxes for W = 24) by TMA tensor copies with the 128-byte
 // swizzle, so each thread's 64 contiguous bytes (half a row) come out of shared
 // memory with conflict-free 16-byte loads in natural order.  The final partial
 // row (if any) is not covered by the tensor; its owner patches it from global
@@ -12,7 +13,7 @@
 // (the few bytes it copies out come from global memory, still in L2).
 //
 // Schedule.  A cooperative persistent grid; CTA b owns tiles b, b+G, ... Each CTA
-// runs 16 worker warps and one manager warp; they hand work to each other through
+// runs W worker warps and one manager warp; they hand work to each other through
 // mbarriers, never through a CTA-wide barrier inside the tile loop.
 //
 //   workers  A(k): wait FULL[k%2]; classify their two 32-byte words; compose them,
@@ -24,7 +25,7 @@
 //            order A(0), A(1), A(2), then A(k+3), B(k) for k = 0, 1, ...: the
 //            class planes of four tiles live in registers, so a tile's totals are
 //            published three tiles before its base is needed.
-//   manager  agg(k):  wait TOT[k%4] -> scan the 16 warp totals -> publish the tile's
+//   manager  agg(k):  wait TOT[k%4] -> scan the W warp totals -> publish the tile's
 //                     AGG word (counts under both in-string hypotheses, parity).
 //            fold(k): reduce the AGG words of the G-1 tiles since this CTA's
 //                     previous tile, combine with the CTA's own running prefix,
@@ -58,11 +59,21 @@ using namespace scan_detail;
 
 namespace {
 
-constexpr int kWorkers	 = 16;
-constexpr int kWsThreads = (kWorkers + 1) * 32;
-constexpr int kMgr		 = kWorkers;				  // warp index of the manager
-constexpr int kWsTile	 = kWorkers * 32 * 64;		  // 32 KiB: 512 threads x 64 bytes
-constexpr int kWsRows	 = kWsTile / 128;			  // 256 rows of 128 bytes
+// The tile shape follows the worker count W: W warps x 32 threads x 64 bytes, so
+// 16 workers scan 32 KiB tiles and 24 workers 48 KiB tiles.
+template<int W>
+struct WsGeom {
+	static constexpr int kWorkers = W;
+	static constexpr int kThreads = (W + 1) * 32;	  // workers + the manager warp
+	static constexpr int kTile	  = W * 32 * 64;
+	static constexpr int kRows	  = kTile / 128;	  // rows of 128 bytes
+	// rows per TMA box (at most 256): a tile is one box, or two
+	static constexpr int kBoxRows = kRows <= 256 ? kRows : kRows / 2;
+	static_assert(kRows % kBoxRows == 0 && kBoxRows <= 256 && kBoxRows % 8 == 0,
+				  "a tile is whole TMA boxes of whole 128-byte swizzle periods");
+	static_assert(kTile < 65536, "per-tile counts travel as 16-bit halves");
+	static_assert(W <= 32, "the manager scans the worker totals in one warp");
+};
 constexpr int kAhead	 = 3;						  // workers run phase A this many tiles ahead of B
 constexpr int kBufs		 = 4;						  // hand-off buffers (>= kAhead + 1)
 constexpr int kListCap	 = 512;						  // listed structurals per warp and tile (bracket kernels)
@@ -85,7 +96,7 @@ __device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, std::uint32_t pari
 	return true;
 }
 
-// 2-D TMA: rows [row, row + 256) of the tensor into `dst` (1024-byte aligned).
+// 2-D TMA: one box of rows starting at `row` of the tensor into `dst` (1024-byte aligned).
 __device__ __forceinline__ void tma_rows(void* dst, const CUtensorMap* map, int row,
 										 std::uint64_t* bar) {
 	asm volatile(
@@ -95,7 +106,8 @@ __device__ __forceinline__ void tma_rows(void* dst, const CUtensorMap* map, int 
 		: "memory");
 }
 
-struct WsScratch {
+template<int kWorkers>
+struct WsScratchT {
 	uint4		  tagg[kBufs];				 // tile aggregates between agg and fold (manager)
 	std::uint32_t wtot[kBufs][kWorkers][4];	 // worker warp aggregates (workers -> manager)
 	std::uint32_t wpre[kBufs][kWorkers][4];	 // worker warp exclusive prefixes (manager -> workers)
@@ -122,16 +134,22 @@ struct WsFront {
 };
 
 // Dynamic shared memory (window addresses): [scratch, histogram, structural lists]
-// [pad to 64 KiB][class table 64 KiB][ring 2 x 32 KiB].  The table and ring start on 64 KiB and
+// [pad to 64 KiB][class table 64 KiB][ring 2 x tile].  The table and ring start on 64 KiB and
 // 1 KiB boundaries of the shared window respectively.
-struct SmemWs {
+template<int kWorkers>
+struct SmemWsT {
+	static constexpr int kWsTile   = WsGeom<kWorkers>::kTile;
 	static constexpr int kBars	   = 0;	 // full[2] tot[4] base[4]
 	static constexpr int kScratch  = 128;
-	static constexpr int kHist	   = (kScratch + static_cast<int>(sizeof(WsScratch)) + 127) & ~127;
+	static constexpr int kHist	   = (kScratch + static_cast<int>(sizeof(WsScratchT<kWorkers>)) + 127) & ~127;
 	static constexpr int kList	   = kHist + 2 * kKeyWindow * 4;	// per-warp structural lists
 	static constexpr int kLowEnd   = kList + kWorkers * kListCap * 2;
 	static constexpr int kTblBytes = 256 * 256;
-	static constexpr int kBytes	   = kLowEnd + 65535 + kTblBytes + 2 * kWsTile;
+	// the table sits on the first 64 KiB boundary of the window (the scratch below
+	// it), the ring right after it; dynamic shared memory starts within the window's
+	// first KiB, so that boundary is 64 KiB into it
+	static constexpr int kBytes	   = 0x10000 + kTblBytes + 2 * kWsTile;
+	static_assert(kLowEnd + 1024 <= 0x10000, "scratch must fit below the table");
 };
 
 struct OpSum3 {
@@ -331,9 +349,17 @@ struct WsItem {
 	bool			   first, last;
 };
 
-template<int PATH, bool BR, bool BATCH>
-__global__ void __launch_bounds__(kWsThreads, 1)
+template<int PATH, bool BR, bool BATCH, int W>
+__global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 	k_scan_ws(const WsArgs wa, const __grid_constant__ CUtensorMap tmap) {
+	constexpr int kWorkers	 = W;
+	constexpr int kWsThreads = WsGeom<W>::kThreads;
+	constexpr int kMgr		 = W;  // warp index of the manager
+	constexpr int kWsTile	 = WsGeom<W>::kTile;
+	constexpr int kWsRows	 = WsGeom<W>::kRows;
+	constexpr int kWsBoxRows = WsGeom<W>::kBoxRows;
+	using WsScratch			 = WsScratchT<W>;
+	using SmemWs			 = SmemWsT<W>;
 	const ScanArgs&	 a	= wa.a;
 	const BatchDesc& bd = wa.bd;
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -665,7 +691,10 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 			} else {
 				// rows past the tensor's end come back as zeros (and count as delivered)
 				mbar_arrive_expect_tx(&full_bar[s], kWsTile);
-				tma_rows(ring + s * kWsTile, &tmap, static_cast<int>(row0), &full_bar[s]);
+#pragma unroll
+				for (int b = 0; b < kWsRows / kWsBoxRows; ++b)
+					tma_rows(ring + s * kWsTile + b * kWsBoxRows * 128, &tmap,
+							 static_cast<int>(row0) + b * kWsBoxRows, &full_bar[s]);
 			}
 		};
 		if (warp == 0 && lane == 0) {

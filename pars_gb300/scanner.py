@@ -210,17 +210,19 @@ class Scanner:
         return BatchView(r) if host_view else r
 
     def autotune(self, d_ptr: int, n: int, want_pairs: bool = False, stream: int = 0) -> dict:
-        """pars_autotune on a sample document: the grid sizes tried, their times, the pick."""
+        """pars_autotune on a sample document: the (workers, grid) pairs tried, their
+        times, the pick."""
         rep = _lib.TuneReport()
         flags = PARS_RUN_PAIRS | (PARS_WANT_PAIRS if want_pairs else 0)
         check(lib().pars_autotune(self.ctx.handle, self.plan_id, ctypes.c_void_p(d_ptr), n, flags,
                                   ctypes.c_void_p(stream), ctypes.byref(rep)), self.ctx.handle)
         k = rep.n_candidates
-        return {"path": rep.path, "bucket": rep.bucket, "grid": rep.grid,
-                "candidates": list(rep.cand_grid[:k]), "ms": [round(x, 4) for x in rep.cand_ms[:k]]}
+        return {"path": rep.path, "bucket": rep.bucket, "grid": rep.grid, "workers": rep.workers,
+                "candidates": list(rep.cand_grid[:k]), "workers_tried": list(rep.cand_workers[:k]),
+                "ms": [round(x, 4) for x in rep.cand_ms[:k]]}
 
-    def tune_set(self, n: int, grid: int) -> None:
-        check(lib().pars_tune_set(self.ctx.handle, self.plan_id, n, grid), self.ctx.handle)
+    def tune_set(self, n: int, grid: int, workers: int = 0) -> None:
+        check(lib().pars_tune_set(self.ctx.handle, self.plan_id, n, grid, workers), self.ctx.handle)
 
     def scan_tensor(self, t, **kw) -> DeviceResult:
         """scan_device on a contiguous uint8 CUDA tensor."""
