@@ -51,8 +51,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel: str):
-    """Per-launch DRAM bytes recorded from an ncu capture (profiles/*.txt), or None."""
+def traffic_from_profiles(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` on `workload` recorded from an ncu capture
+    (profiles/*.txt), or None."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
@@ -60,11 +61,12 @@ def traffic_from_profiles(kernel: str):
         if not fn.endswith(".txt"):
             continue
         for line in open(os.path.join(d, fn)):
-            if line.startswith("traffic_per_launch ") and kernel in line:
-                # traffic_per_launch <kernel> <workload> <bytes>
-                parts = line.split()
+            parts = line.split()
+            # traffic_per_launch <kernel> <workload> <bytes>
+            if len(parts) == 4 and parts[0] == "traffic_per_launch" and parts[1] == kernel \
+                    and parts[2] == workload:
                 try:
-                    return int(float(parts[-1]))
+                    return int(float(parts[3]))
                 except ValueError:
                     return None
     return None
@@ -512,7 +514,7 @@ def main():
                        "n_struct": r.n_struct, "kernel_path": r.kernel_path},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": traffic_from_profiles("k_scan_ws"),
+                         "traffic": traffic_from_profiles("k_scan_ws", "csv_1GiB_single_document"),
                          "peak_kind": peak_kind, "kernel": "k_scan_ws<doubled>",
                          "kernel_ms": round(scan_ms, 4), "algorithmic_bytes": int(alg_bytes)},
             "e2e": e2e,
