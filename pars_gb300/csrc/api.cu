@@ -45,6 +45,7 @@ const void* scan_ws_batch_kernel(int path, bool brackets);
 int		   scan_ws_smem_bytes(int shape);
 const void* scan_ws_kernel(int path, bool brackets, int shape);
 int		   sort_tile_keys();
+const void* r6_kernel(int which);
 const void* bchar_gather_kernel();
 struct SortPass;
 __global__ void k_sort_pass(const SortPass p);
@@ -586,30 +587,46 @@ PairArgs pair_args(pars_ctx* ctx, const Plan* pl, uint32_t flags, const uint32_t
 	return p;
 }
 
+// R6 without a host round-trip: the common-case sort (k_r6_count, k_r6_offsets,
+// k_r6_scatter) and k_pair, which skip themselves when the case does not hold
+// (sort_ok = 0: the host then runs pairs_fallback).
 int launch_pairs_speculative(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t st) {
 	const uint64_t ntiles_sort = (ctx->cap_b + sort_tile_keys() - 1) / sort_tile_keys() + 1;
 	if (int r = grow(ctx, ctx->lb, ntiles_sort * 256 * sizeof(uint64_t)))
 		return r;
-	SortPass sp {};
-	sp.keys_in	  = static_cast<const int32_t*>(ctx->depth.p);
-	sp.idx_out	  = static_cast<uint32_t*>(ctx->order.p);
-	sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
-	sp.ctr		  = ctx->ctr;
-	sp.res		  = ctx->res;
-	sp.key_hist	  = ctx->key_hist;
-	sp.cap		  = ctx->cap_b;
-	sp.epoch	  = next_epoch(ctx);
-	sp.first	  = 1;
+	if (int r = grow(ctx, ctx->sort_keys_a, ctx->cap_b * 4 + 16))
+		return r;
+	if (int r = grow(ctx, ctx->sort_keys_b, ctx->cap_b + 16))
+		return r;
+	if (int r = grow(ctx, ctx->sort_idx_b, ctx->cap_b * 4 + 16))
+		return r;
+	R6Sort rs {};
+	rs.keys		 = static_cast<const int32_t*>(ctx->depth.p);
+	rs.bsi		 = static_cast<const uint32_t*>(ctx->bsi.p);
+	rs.bpos		 = static_cast<const uint32_t*>(ctx->bpos.p);
+	rs.in		 = ctx->cur_in;
+	rs.bchar	 = static_cast<uint8_t*>(ctx->bchar.p);
+	rs.tile_cnt	 = static_cast<uint32_t*>(ctx->lb.p);
+	rs.order	 = static_cast<uint32_t*>(ctx->order.p);
+	rs.sorted_si = static_cast<uint32_t*>(ctx->sort_keys_a.p);
+	rs.sorted_ch = static_cast<uint8_t*>(ctx->sort_keys_b.p);
+	rs.rank_of	 = static_cast<uint32_t*>(ctx->sort_idx_b.p);
+	rs.res		 = ctx->res;
+	rs.key_hist	 = ctx->key_hist;
+	rs.cap		 = ctx->cap_b;
+	rs.tiles_cap = ctx->lb.cap / (256 * sizeof(uint32_t));
+	void*	  a1[] = {&rs};
 	const int grid = ctx->num_sms * 4;
-	void*	  a1[] = {&sp};
-	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(grid), dim3(256), a1, 0,
-						st));
-	ctx->launches++;
+	CK(cudaLaunchKernel(r6_kernel(0), dim3(grid), dim3(256), a1, 0, st));
+	CK(cudaLaunchKernel(r6_kernel(1), dim3(256), dim3(1024), a1, 0, st));
+	CK(cudaLaunchKernel(r6_kernel(2), dim3(grid), dim3(256), a1, 0, st));
+	ctx->launches += 3;
 	PairArgs pa	  = pair_args(ctx, pl, flags, static_cast<const uint32_t*>(ctx->order.p));
-	int		 req  = 1;
-	void*	 a2[] = {&pa, &req};
-	CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pair), dim3(ctx->num_sms * 4), dim3(256), a2,
-						0, st));
+	pa.sorted_si  = rs.sorted_si;
+	pa.sorted_ch  = rs.sorted_ch;
+	pa.rank_of	  = rs.rank_of;
+	void* a2[] = {&pa};
+	CK(cudaLaunchKernel(r6_kernel(3), dim3(ctx->num_sms * 4), dim3(256), a2, 0, st));
 	ctx->launches++;
 	return 0;
 }
@@ -782,8 +799,12 @@ int scan_device_impl(pars_ctx* ctx, Plan* pl, const uint8_t* d_in, uint64_t n, u
 	for (int attempt = 0; attempt < 4; ++attempt) {
 		if (int r = ensure_outputs(ctx, want_s, want_b, n, flags))
 			return r;
-		Scan s {d_in, n, flags, st, path, nullptr, nullptr};
-		ctx->cur_in = d_in;
+		// With R6 the warp-specialised scan writes each bracket's byte itself while
+		// the tile is fresh in L2; R6 then reads them in order instead of gathering
+		// them from a document the outputs have pushed out of L2.
+		const bool own = run_pairs && use_ws(path);
+		Scan	   s {d_in, n, flags | (own ? kScanOwnBchar : 0u), st, path, nullptr, nullptr};
+		ctx->cur_in = own ? nullptr : d_in;
 		if (ctx->profiling)
 			CK(cudaEventRecord(ctx->prof[0], st));
 		if (int r = launch_scan(ctx, pl, s))

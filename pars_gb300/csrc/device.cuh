@@ -106,14 +106,20 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(std::uint64_t* bar, std::u
 				 : "memory");
 }
 
+// One bounded poll of phase `phase` of `bar`.  The explicit suspend-time hint (in
+// ns) caps how long the thread sleeps inside one try_wait, so a caller's spin
+// limit bounds its wall time (kSpinLimit polls of at most kWaitHintNs each) instead
+// of a system-dependent default.
+constexpr std::uint32_t kWaitHintNs = 1000;
+
 __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, std::uint32_t phase) {
 	std::uint32_t ok;
 	asm volatile(
 		"{\n\t.reg .pred p;\n\t"
-		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
 		"selp.u32 %0, 1, 0, p;\n\t}"
 		: "=r"(ok)
-		: "r"(smem_addr(bar)), "r"(phase)
+		: "r"(smem_addr(bar)), "r"(phase), "n"(kWaitHintNs)
 		: "memory");
 	return ok != 0;
 }

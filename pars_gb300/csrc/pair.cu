@@ -15,9 +15,17 @@
 //                bracket index;
 //   k_digit_hist the digit histogram for passes the scan's window cannot provide;
 //   k_pair       adjacent pairing + type check, then the last CTA folds the flags.
-// The common case (key range <= 256, all keys in the window) is ONE sort pass
-// launched without a host round-trip; anything else is finished by the host with
-// LSD passes over 8-bit digits.
+// The common case (key range <= 256, all keys in the window) runs without a host
+// round-trip and without look-back chains:
+//   k_r6_count    per-tile digit counts (tiles of 4096 keys, warp match-any);
+//   k_r6_offsets  per digit, the exclusive scan of its counts over tiles plus the
+//                 digit's global base (from the scan's key histogram);
+//   k_r6_scatter  stable ranks again, each bracket to its sorted slot, with its
+//                 structural index and byte beside it, and its slot recorded;
+//   k_pair_ranked each bracket reads its partner's slot and writes its own
+//                 entries in order (no scattered writes).
+// Anything else is finished by the host with k_sort_pass LSD passes over 8-bit
+// digits.
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -212,6 +220,190 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(const SortPass p) {
 	}
 }
 
+namespace {
+
+// The common case holds: every key in the window, the range within one digit, the
+// outputs within capacity.  Writes sort_ok (block 0, thread 0).
+__device__ __forceinline__ bool r6_common(const R6Sort& p, unsigned long long& n, long long& kmin,
+										  unsigned int& nb) {
+	DevResult* res = p.res;
+	n			   = res->n_brackets;
+	const bool has = n && res->min_key && res->max_key;
+	kmin		   = has ? dec_min(res->min_key) : 0;
+	const long long kmax  = has ? dec_max(res->max_key) : 0;
+	const long long range = has ? kmax - kmin + 1 : 0;
+	const unsigned long long tiles = (n + kSortTile - 1) / kSortTile;
+	const bool ok = !res->keys_oob && !res->error && n <= p.cap && tiles <= p.tiles_cap
+				 && (n == 0 || (has && range >= 1 && range <= 256 && kmin >= -kKeyWindow && kmax < kKeyWindow));
+	nb = static_cast<unsigned int>(range);
+	return ok;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kSortThreads) k_r6_count(const R6Sort p) {
+	__shared__ unsigned int hist[256];
+	unsigned long long		n;
+	long long				kmin;
+	unsigned int			nb;
+	const bool				ok = r6_common(p, n, kmin, nb);
+	const int				tid = threadIdx.x;
+	if (blockIdx.x == 0 && tid == 0)
+		p.res->sort_ok = ok ? 1u : 0u;
+	if (!ok || n == 0)
+		return;
+	const unsigned long long tiles = (n + kSortTile - 1) / kSortTile;
+	for (unsigned long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+		// every key of the thread in flight at once, then the counting
+		std::uint32_t dg[kSortItems];
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = t * kSortTile + static_cast<unsigned long long>(i) * kSortThreads + tid;
+			dg[i] = e < n ? static_cast<std::uint32_t>(p.keys[e] - kmin) : 0xFFFFFFFFu;
+		}
+		hist[tid] = 0;
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const std::uint32_t d	  = dg[i];
+			const std::uint32_t peers = __match_any_sync(kFull, d);
+			if (d != 0xFFFFFFFFu && (peers & ((1u << (tid & 31)) - 1u)) == 0)
+				atomicAdd(&hist[d], static_cast<unsigned int>(__popc(peers)));
+		}
+		__syncthreads();
+		if (static_cast<unsigned int>(tid) < nb)
+			p.tile_cnt[static_cast<unsigned long long>(tid) * tiles + t] = hist[tid];
+		__syncthreads();
+	}
+}
+
+// One block per digit: global base + exclusive scan of the digit's tile counts.
+__global__ void __launch_bounds__(1024) k_r6_offsets(const R6Sort p) {
+	__shared__ unsigned int wsum[32];
+	__shared__ unsigned int s_carry;
+	unsigned long long		n;
+	long long				kmin;
+	unsigned int			nb;
+	if (!r6_common(p, n, kmin, nb) || n == 0 || blockIdx.x >= nb)
+		return;
+	const int		   tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const unsigned int d   = blockIdx.x;
+	// the digit's global base: brackets with a smaller key
+	unsigned int c = 0;
+	if (static_cast<unsigned int>(tid) < d)
+		c = p.key_hist[kmin + tid + kKeyWindow];
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+	if (lane == 0)
+		wsum[warp] = c;
+	__syncthreads();
+	if (tid == 0) {
+		unsigned int b = 0;
+		for (int w = 0; w < 32; ++w) b += wsum[w];
+		s_carry = b;
+	}
+	__syncthreads();
+	const unsigned long long tiles = (n + kSortTile - 1) / kSortTile;
+	std::uint32_t*			 row   = p.tile_cnt + static_cast<unsigned long long>(d) * tiles;
+	for (unsigned long long t0 = 0; t0 < tiles; t0 += 1024) {
+		const unsigned long long t = t0 + tid;
+		const unsigned int		 v = t < tiles ? row[t] : 0u;
+		unsigned int			 x = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const unsigned int y = __shfl_up_sync(kFull, x, o);
+			if (lane >= o)
+				x += y;
+		}
+		if (lane == 31)
+			wsum[warp] = x;
+		__syncthreads();
+		unsigned int wp = 0;
+		for (int w = 0; w < warp; ++w) wp += wsum[w];
+		const unsigned int carry = s_carry;
+		if (t < tiles)
+			row[t] = carry + wp + x - v;
+		__syncthreads();
+		if (tid == 1023)
+			s_carry = carry + wp + x;
+		__syncthreads();
+	}
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_r6_scatter(const R6Sort p) {
+	__shared__ unsigned int whist[kSortWarps][256];
+	unsigned long long		n;
+	long long				kmin;
+	unsigned int			nb;
+	if (!r6_common(p, n, kmin, nb) || n == 0)
+		return;
+	const int				 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const unsigned long long tiles = (n + kSortTile - 1) / kSortTile;
+	for (unsigned long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+		// warp w ranks 512 consecutive keys, 16 rounds of 32 (stable within the tile).
+		// First every load of the thread goes out at once: keys, structural
+		// indices, byte offsets, then the bracket bytes (independent gathers whose
+		// latency the ranking below overlaps).
+		const unsigned long long wbase = t * kSortTile + static_cast<unsigned long long>(warp) * 512;
+		std::uint32_t			 dig[kSortItems], rnk[kSortItems], sis[kSortItems];
+		std::uint8_t			 chs[kSortItems];
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			dig[i]					   = e < n ? static_cast<std::uint32_t>(p.keys[e] - kmin) : 0xFFFFFFFFu;
+			sis[i]					   = e < n ? p.bsi[e] : 0u;
+			rnk[i]					   = e < n && p.in ? p.bpos[e] : 0u;
+		}
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			chs[i]					   = e < n ? (p.in ? p.in[rnk[i]] : p.bchar[e]) : std::uint8_t(0);
+		}
+		for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const std::uint32_t		 d	   = dig[i];
+			const std::uint32_t		 peers = __match_any_sync(kFull, d);
+			const std::uint32_t		 below = peers & ((1u << lane) - 1u);
+			std::uint32_t			 base  = 0;
+			if (d != 0xFFFFFFFFu)
+				base = whist[warp][d];
+			__syncwarp();
+			if (d != 0xFFFFFFFFu && below == 0)
+				whist[warp][d] = base + __popc(peers);
+			__syncwarp();
+			rnk[i] = base + __popc(below);
+		}
+		__syncthreads();
+		// digit offsets: the tile's (from k_r6_offsets) plus the earlier warps'
+		if (static_cast<unsigned int>(tid) < nb) {
+			unsigned int off = p.tile_cnt[static_cast<unsigned long long>(tid) * tiles + t];
+			for (int w = 0; w < kSortWarps; ++w) {
+				const unsigned int c = whist[w][tid];
+				whist[w][tid]		 = off;
+				off += c;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			const std::uint32_t		 d = dig[i];
+			if (d == 0xFFFFFFFFu)
+				continue;
+			const std::uint32_t dst = whist[warp][d] + rnk[i];
+			if (dst >= n)
+				continue;  // unreachable while the key histogram matches the keys
+			if (p.in)
+				p.bchar[e] = chs[i];
+			p.rank_of[e]	 = dst;
+			p.order[dst]	 = static_cast<std::uint32_t>(e);
+			p.sorted_si[dst] = sis[i];
+			p.sorted_ch[dst] = chs[i];
+		}
+		__syncthreads();
+	}
+}
+
 // Histogram of one 8-bit digit of key - min_key (host-driven LSD passes).
 __global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, unsigned int shift,
 							 unsigned int* hist) {
@@ -230,6 +422,39 @@ __global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, uns
 	if (h[threadIdx.x])
 		atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
+
+namespace {
+
+// A block's mismatches go to the result; the last block to finish folds the flags.
+__device__ __forceinline__ void pair_finish(const PairArgs& a, unsigned int bad, unsigned int& s_bad,
+											unsigned long long n) {
+	DevResult* res = a.res;
+	const int  tid = threadIdx.x;
+	if (__any_sync(kFull, bad) && (tid & 31) == 0)
+		atomicOr(&s_bad, 1u);
+	__syncthreads();
+	if (tid == 0) {
+		if (s_bad)
+			atomicOr(&res->mismatch, 1u);
+		__threadfence();
+		const unsigned int done = atomicAdd(&a.ctr->pair_done, 1u);
+		if (done == gridDim.x - 1) {
+			__threadfence();
+			const long long	 fin = static_cast<long long>(res->n_open) - static_cast<long long>(res->n_close);
+			const long long	 mnb = res->min_bal ? dec_min(res->min_bal) : 0;
+			const long long	 mxb = res->max_bal ? dec_max(res->max_bal) : 0;
+			const bool		 bal = mnb >= 0 && fin == 0;
+			const unsigned int mis = *reinterpret_cast<volatile unsigned int*>(&res->mismatch);
+			res->balanced		 = bal ? 1u : 0u;
+			res->well_formed	 = (bal && !mis && (n % 2 == 0)) ? 1u : 0u;
+			res->max_depth		 = static_cast<int>(mxb > 0 ? mxb : 0);
+			a.ctr->pair_done	 = 0;
+			__threadfence();
+		}
+	}
+}
+
+}  // namespace
 
 // Adjacent pairing over the sorted order, then flags (last CTA).
 __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort_ok) {
@@ -291,28 +516,59 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs a, int require_sort
 			}
 		}
 	}
-	if (__any_sync(kFull, bad) && (tid & 31) == 0)
-		atomicOr(&s_bad, 1u);
+	pair_finish(a, bad, s_bad, n);
+}
+
+// Pairing in bracket order from the common-case sort: bracket i sits at sorted
+// position q = rank_of[i] and is paired with the entry at q ^ 1 (the reference's
+// order[2k] with order[2k+1]), whose index, structural index and byte k_r6_scatter
+// laid out at that position.  Every bracket writes its own bpair entry and its own
+// structural entry, in order; the reads at q ^ 1 are the only scattered accesses.
+__global__ void __launch_bounds__(256) k_pair_ranked(const PairArgs a) {
+	__shared__ std::uint8_t	 s_open[256], s_close[256];
+	__shared__ std::uint16_t s_first[256];
+	__shared__ unsigned int	 s_bad;
+	DevResult* res = a.res;
+	const int  tid = threadIdx.x;
+	if (!res->sort_ok)
+		return;
+	s_open[tid]	 = a.plan->is_open[tid];
+	s_close[tid] = a.plan->is_close[tid];
+	s_first[tid] = a.plan->first_close[tid];
+	if (tid == 0)
+		s_bad = 0;
 	__syncthreads();
-	if (tid == 0) {
-		if (s_bad)
-			atomicOr(&res->mismatch, 1u);
-		__threadfence();
-		const unsigned int done = atomicAdd(&a.ctr->pair_done, 1u);
-		if (done == gridDim.x - 1) {
-			__threadfence();
-			const long long	 fin = static_cast<long long>(res->n_open) - static_cast<long long>(res->n_close);
-			const long long	 mnb = res->min_bal ? dec_min(res->min_bal) : 0;
-			const long long	 mxb = res->max_bal ? dec_max(res->max_bal) : 0;
-			const bool		 bal = mnb >= 0 && fin == 0;
-			const unsigned int mis = *reinterpret_cast<volatile unsigned int*>(&res->mismatch);
-			res->balanced		 = bal ? 1u : 0u;
-			res->well_formed	 = (bal && !mis && (n % 2 == 0)) ? 1u : 0u;
-			res->max_depth		 = static_cast<int>(mxb > 0 ? mxb : 0);
-			a.ctr->pair_done	 = 0;
-			__threadfence();
+	const unsigned long long n = res->n_brackets;
+	if (n > a.cap_b || res->n_struct > a.cap_s)
+		return;	 // outputs overflowed: the host grows the buffers and reruns
+	const bool	 want = (a.flags & 1u) != 0;
+	unsigned int bad  = 0;
+	for (unsigned long long i = blockIdx.x * 256ull + tid; i < n; i += gridDim.x * 256ull) {
+		const std::uint32_t		 q	= a.rank_of[i];
+		const unsigned long long pq = q ^ 1u;
+		std::int32_t			 bp = -1, sp = -1;
+		if (pq < n) {
+			const std::uint32_t j  = a.order[pq];
+			const std::uint32_t sj = a.sorted_si[pq];
+			const std::uint8_t	cj = a.sorted_ch[pq];
+			const std::uint8_t	ci = a.bchar[i];
+			const std::uint8_t	co = (q & 1u) ? cj : ci, cc = (q & 1u) ? ci : cj;  // order[2k], order[2k+1]
+			const bool			ok = s_open[co] && s_close[cc] && s_first[co] == (0x100u | cc);
+			if (ok) {
+				bp = static_cast<std::int32_t>(j);
+				sp = static_cast<std::int32_t>(sj);
+			} else {
+				bad = 1;
+			}
+		}
+		if (want) {
+			if (a.bpair)
+				a.bpair[i] = bp;
+			if (a.pair)
+				a.pair[a.bsi[i]] = sp;
 		}
 	}
+	pair_finish(a, bad, s_bad, n);
 }
 
 // Bracket bytes gathered from the document when R6 does not run.
@@ -329,6 +585,16 @@ const void* bchar_gather_kernel() {
 
 int sort_tile_keys() {
 	return kSortTile;
+}
+
+const void* r6_kernel(int which) {
+	switch (which) {
+		case 0: return reinterpret_cast<const void*>(&k_r6_count);
+		case 1: return reinterpret_cast<const void*>(&k_r6_offsets);
+		case 2: return reinterpret_cast<const void*>(&k_r6_scatter);
+		case 3: return reinterpret_cast<const void*>(&k_pair_ranked);
+		default: return nullptr;
+	}
 }
 
 }  // namespace pars

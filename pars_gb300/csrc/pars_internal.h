@@ -232,6 +232,26 @@ struct ScanArgs {
 	unsigned int		 flags;
 };
 
+// The common-case R6 sort (every key in the window, key range <= 256): per-tile
+// digit histograms, a per-digit scan over tiles, then a stable scatter that also
+// lays out each bracket's structural index and byte in sorted order for k_pair.
+struct R6Sort {
+	const std::int32_t*	 keys;		// [n] depth keys
+	const std::uint32_t* bsi;		// [n] structural indices
+	const std::uint32_t* bpos;		// [n] byte offsets (with `in`)
+	const std::uint8_t*	 in;		// the document, or null: the scan wrote bchar
+	std::uint8_t*		 bchar;		// [n] bracket bytes: written (with `in`) or read
+	std::uint32_t*		 tile_cnt;	// [256][tiles] per-tile digit counts, then offsets
+	std::uint32_t*		 order;		// [n] bracket indices sorted by (key, index)
+	std::uint32_t*		 sorted_si; // [n] structural index of order[p]
+	std::uint8_t*		 sorted_ch; // [n] bracket byte of order[p]
+	std::uint32_t*		 rank_of;	// [n] sorted position of bracket i (order's inverse)
+	DevResult*			 res;
+	const unsigned int*	 key_hist;	// [2048] window histogram from the scan
+	unsigned long long	 cap;		// capacity of the bracket arrays
+	unsigned long long	 tiles_cap; // tiles the tile_cnt buffer holds
+};
+
 struct PairArgs {
 	const std::int32_t*	 depth;		// [n_brackets] keys
 	const std::uint8_t*	 bchar;		// bracket bytes written by the scan (when `in` is null)
@@ -242,6 +262,9 @@ struct PairArgs {
 	std::uint32_t*		 order;		// [n_brackets] bracket indices sorted by (key, index)
 	std::int32_t*		 pair;		// structural space, may be null
 	std::int32_t*		 bpair;		// bracket space, may be null
+	const std::uint32_t* sorted_si; // with R6Sort: structural index and byte of order[p],
+	const std::uint8_t*	 sorted_ch; // and the sorted position of each bracket
+	const std::uint32_t* rank_of;
 	std::uint64_t*		 sort_tiles;
 	Counters*			 ctr;
 	DevResult*			 res;
