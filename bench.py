@@ -244,6 +244,29 @@ def time_device(sc, t, steps, warmup, stream, want_pairs, dist_barrier):
         launches, r
 
 
+def general_leg(ctx, stream, barrier, peak, nbytes=64 << 20, steps=10):
+    """The multi-descriptor grammars on the general kernel: one 64 MiB seeded
+    document each (device-resident, R6 included where the grammar has brackets)."""
+    import torch
+    from pars_gb300 import Scanner, synth
+    out = []
+    for g in ("toml", "clike", "ini", "xml"):
+        data = synth.config_doc(g, SEED, nbytes)
+        t = torch.from_numpy(data).cuda()
+        sc = Scanner(plan(g), ctx=ctx)
+        ms, scan_ms, pair_ms, launches, r = time_device(sc, t, steps, 3, stream, True, barrier)
+        alg = data.size + 8 * r.n_struct + 4 * r.n_brackets
+        out.append({"grammar": g, "bytes": int(data.size), "GBps": round(data.size / (ms / 1e3) / 1e9, 3),
+                    "ms_per_step": round(ms, 4), "scan_kernel_ms": round(scan_ms, 4),
+                    "pair_kernels_ms": round(pair_ms, 4), "n_struct": int(r.n_struct),
+                    "n_brackets": int(r.n_brackets), "kernel_path": r.kernel_path,
+                    "roofline_pipeline_frac": round(alg / (ms / 1e3) / 1e9 / peak, 4),
+                    "gpu_launches_per_step": launches / steps})
+        del t
+    return {"workload": "general_path_64MiB_documents", "data": "synthetic (synth.config_doc)",
+            "documents": out}
+
+
 def batched_leg(args, stream, barrier, world, peak, ndocs=100_000, sample=2000):
     """Batched JSON (100,000 documents, log-normal sizes: median 2 KiB, sigma 1.5,
     clamped to 64 B - 4 MiB): one pars_scan_batch call per step (device-resident
@@ -491,6 +514,10 @@ def main():
         }
         del jt
 
+    general = None
+    if not args.no_secondary:
+        general = general_leg(sc.ctx, stream, barrier, peak)
+
     batched = None
     if not args.no_batched:
         batched = batched_leg(args, stream, barrier, world, peak)
@@ -522,6 +549,7 @@ def main():
             "clocks": clocks,
             "cpu_baseline": cpu,
             "secondary": secondary,
+            "general_path": general,
             "batched": batched,
             "serving": serving,
         }

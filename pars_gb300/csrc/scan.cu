@@ -364,8 +364,10 @@ struct SmemLayout {
 // ============================================================================
 // The scan kernel.  PATH selects the R4 algebra; everything else is shared.
 // ============================================================================
+// Two CTAs per SM (64 registers, about 92 KB of shared memory each): a tile's two
+// look-back chains wait in one CTA while the other classifies.
 template<int PATH>
-__global__ void __launch_bounds__(kScanThreads, 1) k_scan(const ScanArgs a) {
+__global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	extern __shared__ __align__(128) unsigned char smem[];
 	std::uint32_t*	 tbl	= reinterpret_cast<std::uint32_t*>(smem + SmemLayout::kTbl);
 	unsigned char*	 stages = smem + SmemLayout::kStage;

@@ -8,6 +8,8 @@
 //                      byte budget; containers still open at the budget are closed,
 //                      so the output is always one well-formed top-level array.
 //   pars_synth_csv   — RFC-4180-style CSV with LF records and quoted fields.
+//   pars_synth_config — TOML / C-like / INI / XML documents mixing every lexical
+//                      mode of the grammar with structural bytes in and out of them.
 //   pars_synth_alpha — uniform random bytes over an alphabet (adversarial inputs).
 #include <cmath>
 #include <cstdint>
@@ -339,6 +341,191 @@ std::uint64_t pars_synth_csv(std::uint64_t seed, std::uint64_t target, std::uint
 			}
 		}
 		o.put('\n');
+	}
+	return o.n;
+}
+
+// Documents for the multi-descriptor grammars (kind 0 TOML, 1 C-like, 2 INI, 3 XML).
+// Each mixes every lexical mode of its grammar with the grammar's structural bytes
+// placed both outside and inside those modes (strings, comments), so the general
+// kernel's state carries are exercised at every distance.  Whole records are emitted
+// until the size reaches `target`.
+std::uint64_t pars_synth_config(std::uint64_t seed, int kind, std::uint64_t target, std::uint8_t* out,
+								std::uint64_t cap) {
+	Rng r(seed);
+	Out o {out, cap};
+	auto word = [&](std::uint64_t lo, std::uint64_t hi) {
+		const std::uint64_t len = r.range(lo, hi);
+		for (std::uint64_t i = 0; i < len; ++i) o.put(static_cast<std::uint8_t>(kAlnum[r.range(0, 61)]));
+	};
+	// free text that may carry any of `noise` (structural outside the mode)
+	auto text = [&](std::uint64_t lo, std::uint64_t hi, const char* noise, double p) {
+		const std::uint64_t len	 = r.range(lo, hi);
+		const std::uint64_t nlen = std::strlen(noise);
+		for (std::uint64_t i = 0; i < len; ++i) {
+			if (r.chance(p))
+				o.put(static_cast<std::uint8_t>(noise[r.range(0, nlen - 1)]));
+			else if (r.chance(0.15))
+				o.put(' ');
+			else
+				o.put(static_cast<std::uint8_t>(kAlnum[r.range(0, 61)]));
+		}
+	};
+	while (o.n < target) {
+		const std::uint64_t u = r.range(0, 99);
+		switch (kind) {
+			case 0: {  // TOML
+				if (u < 8) {
+					const bool arr = r.chance(0.3);	 // [[array table]] or [table]
+					o.put(arr ? "[[" : "[");
+					word(3, 10);
+					if (r.chance(0.5)) {
+						o.put('.');
+						word(2, 8);
+					}
+					o.put(arr ? "]]" : "]");
+				} else if (u < 18) {
+					o.put('#');
+					text(0, 40, "{}[],=\"'.", 0.15);
+				} else {
+					word(2, 12);
+					if (r.chance(0.2)) {
+						o.put('.');
+						word(2, 8);
+					}
+					o.put(" = ");
+					const std::uint64_t v = r.range(0, 99);
+					if (v < 30) {
+						o.put('"');
+						const std::uint64_t len = r.range(0, 40);
+						for (std::uint64_t i = 0; i < len; ++i) {
+							const std::uint64_t w = r.range(0, 99);
+							if (w < 4)
+								o.put("\\\"");
+							else if (w < 7)
+								o.put("\\\\");
+							else if (w < 14)
+								o.put(static_cast<std::uint8_t>("{}[],=#'."[r.range(0, 8)]));
+							else
+								o.put(static_cast<std::uint8_t>(kAlnum[r.range(0, 61)]));
+						}
+						o.put('"');
+					} else if (v < 45) {
+						o.put('\'');
+						text(0, 30, "{}[],=#\"\\.", 0.15);
+						o.put('\'');
+					} else if (v < 60) {
+						o.put('[');
+						const std::uint64_t k = r.range(0, 6);
+						for (std::uint64_t i = 0; i < k; ++i) {
+							if (i)
+								o.put(", ");
+							word(1, 6);
+						}
+						o.put(']');
+					} else if (v < 70) {
+						o.put("{ ");
+						word(1, 6);
+						o.put(" = ");
+						word(1, 6);
+						o.put(", ");
+						word(1, 6);
+						o.put(" = \"");
+						text(0, 12, "{},", 0.2);
+						o.put("\" }");
+					} else {
+						word(1, 10);
+					}
+					if (r.chance(0.1)) {
+						o.put(" # ");
+						text(0, 20, "{}[],=\"'", 0.2);
+					}
+				}
+				o.put('\n');
+				break;
+			}
+			case 1: {  // C-like
+				if (u < 15) {
+					o.put("/*");
+					text(0, 60, "{};/\n", 0.1);
+					if (r.chance(0.3))
+						o.put("**");
+					o.put("*/");
+				} else if (u < 30) {
+					o.put("//");
+					text(0, 50, "{};/*", 0.12);
+					o.put('\n');
+				} else if (u < 45) {
+					o.put(r.chance(0.5) ? "{\n" : "}\n");
+				} else {
+					word(1, 10);
+					o.put(' ');
+					word(1, 10);
+					o.put(r.chance(0.7) ? ";\n" : "; ");
+				}
+				break;
+			}
+			case 2: {  // INI
+				if (u < 10) {
+					o.put('[');
+					word(3, 12);
+					o.put("]\n");
+				} else if (u < 25) {
+					o.put(';');
+					text(0, 50, "[]=#", 0.15);
+					o.put('\n');
+				} else if (u < 30) {
+					o.put('\n');
+				} else {
+					word(1, 12);
+					o.put(r.chance(0.5) ? " = " : "=");
+					word(0, 20);
+					o.put('\n');
+				}
+				break;
+			}
+			default: {	// XML
+				if (u < 10) {
+					o.put("<?");
+					word(3, 6);
+					o.put(" v=\"1.0\"?>");
+				} else if (u < 20) {
+					o.put("<!");
+					word(3, 8);
+					o.put(' ');
+					word(1, 10);
+					o.put('>');
+				} else if (u < 55) {
+					o.put('<');
+					word(1, 8);
+					const std::uint64_t na = r.range(0, 3);
+					for (std::uint64_t i = 0; i < na; ++i) {
+						o.put(' ');
+						word(1, 6);
+						o.put('=');
+						if (r.chance(0.6)) {
+							o.put('"');
+							text(0, 20, "<>/='", 0.15);
+							o.put('"');
+						} else {
+							o.put('\'');
+							text(0, 20, "<>/=\"", 0.15);
+							o.put('\'');
+						}
+					}
+					o.put(r.chance(0.2) ? "/>" : ">");
+				} else if (u < 75) {
+					o.put("</");
+					word(1, 8);
+					o.put('>');
+				} else {
+					text(1, 60, ">/='\"&;", 0.08);
+				}
+				if (r.chance(0.3))
+					o.put('\n');
+				break;
+			}
+		}
 	}
 	return o.n;
 }

@@ -14,6 +14,8 @@ workloads used by bench.py and the tests):
   1-64 KiB strings with escape runs (2 GiB stress document).
 * ``csv_doc``   — 16 columns, LF records, unquoted fields U[0,24] alphanumerics,
   10% quoted fields with ',', LF and '""' at 5% per position (1 GiB).
+* ``config_doc`` — TOML / C-like / INI / XML documents for the general-path
+  grammars (64 MiB each in bench.py).
 * ``json_batch`` — many json_doc-style documents with log-normal sizes (median
   2 KiB, sigma 1.5, clamped 64 B - 4 MiB), concatenated with a uint64 offset table.
 """
@@ -41,6 +43,8 @@ def _lib():
         L.pars_synth_json.argtypes = [u64, u64, ctypes.c_int, vp, u64]
         L.pars_synth_csv.restype = u64
         L.pars_synth_csv.argtypes = [u64, u64, vp, u64]
+        L.pars_synth_config.restype = u64
+        L.pars_synth_config.argtypes = [u64, ctypes.c_int, u64, vp, u64]
         L.pars_synth_alpha.restype = None
         L.pars_synth_alpha.argtypes = [u64, vp, u64, vp, u64]
         L.pars_synth_lognormal_sizes.restype = None
@@ -73,6 +77,18 @@ def json_deep(seed: int, target: int) -> np.ndarray:
 def csv_doc(seed: int, target: int) -> np.ndarray:
     return _gen(lambda s, t, p, c: _lib().pars_synth_csv(s, t, p, c), seed, target,
                 target=target, slack=8192)
+
+
+_CONFIG_KINDS = {"toml": 0, "clike": 1, "ini": 2, "xml": 3}
+
+
+def config_doc(grammar: str, seed: int, target: int) -> np.ndarray:
+    """A document for one of the multi-descriptor grammars (toml, clike, ini, xml):
+    every lexical mode (strings, literal strings, comments, tags) with the grammar's
+    structural bytes both inside and outside them."""
+    kind = _CONFIG_KINDS[grammar]
+    return _gen(lambda s, t, p, c: _lib().pars_synth_config(s, kind, t, p, c), seed, target,
+                target=target, slack=4096)
 
 
 def alpha(seed: int, alphabet: bytes, n: int) -> np.ndarray:

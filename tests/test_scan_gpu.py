@@ -139,6 +139,19 @@ def test_unaligned_input(scanners, offset):
         compare(run(scanners[g], data, offset=offset), e, f"{g}/off{offset}", mask=False)
 
 
+@pytest.mark.parametrize("grammar", ["toml", "clike", "ini", "xml"])
+@pytest.mark.parametrize("size", [(3 << 20) + 5, 40 << 20])
+def test_general_grammar_documents(scanners, grammar, size):
+    """Seeded TOML / C-like / INI / XML documents (every lexical mode, structural
+    bytes inside and outside them) on the general path: every output against the
+    oracle, at a small size and at a size spanning hundreds of tiles."""
+    plan = plan_bytes(grammar)
+    data = synth.config_doc(grammar, 31, size)
+    e = expected_from_oracle(plan, data)
+    g = run(scanners[grammar], data)
+    compare(g, e, f"{grammar}/{size}")
+
+
 def test_json_64mib_config(scanners):
     """The single-document JSON workload at its full 64 MiB size."""
     plan = plan_bytes("json")
