@@ -81,6 +81,19 @@ __device__ __forceinline__ std::uint32_t then_map(std::uint32_t X, std::uint32_t
 	return bytes_to_nib(r0, r1);
 }
 
+// Per-byte step tables of the general path (16 B per byte value and descriptor):
+//   x, y: for states 0..3 and 4..7, one byte each: next state | masked << 3
+//   z, w: the next states alone, shifted into the high nibble of each byte.
+// One byte applied to a nibble-packed map in the shuffled layout: the result's
+// nibble sigma(p) holds next[X's nibble p], with sigma(k) = 2k and sigma(4 + k) =
+// 2k + 1 for k < 4.  The two permutes read their selectors straight from X and
+// their outputs interleave into nibbles with one LOP3 (which also drops the masked
+// bits), so no repacking is needed.  sigma has order 3: after a multiple of three
+// steps the layout is the plain one again.
+__device__ __forceinline__ std::uint32_t step_shuffled(std::uint32_t X, const uint4& t) {
+	return (prmt(t.x, t.y, X) & 0x07070707u) | prmt(t.z, t.w, X >> 16);
+}
+
 __device__ __forceinline__ std::uint32_t compose_map(std::uint32_t X, std::uint32_t Y) {
 	std::uint32_t lo, hi;
 	nib_to_bytes(Y, lo, hi);
@@ -104,6 +117,9 @@ struct Scratch {
 };
 
 constexpr int kTableBytes = 256 * 32 * 4;
+// Descriptors with per-byte step tables (the first four); any further descriptors
+// use the class tables.
+constexpr int kByteTabDescs = 4;
 
 // ---- bounded look-back --------------------------------------------------------
 // Waits until tile `idx`'s status carries this launch's epoch and a flag.
@@ -356,7 +372,8 @@ struct SmemLayout {
 	static constexpr int kHist	  = (kScratch + static_cast<int>(sizeof(Scratch)) + 127) & ~127;
 	static constexpr int kGen	  = kHist + 2 * kKeyWindow * 4;	 // generic: rep_of + step tables
 	static constexpr int kBytesFast = kGen;
-	static constexpr int kBytesGen	= kGen + 8 * 256 + 8 * 64 + 2 * 8 * 8 * 4;
+	static constexpr int kBtab		= kGen + 8 * 256 + 8 * 64 + 2 * 8 * 8 * 4;	 // 16-byte aligned
+	static constexpr int kBytesGen	= kBtab + kByteTabDescs * 256 * 16;
 };
 
 }  // namespace
@@ -364,7 +381,7 @@ struct SmemLayout {
 // ============================================================================
 // The scan kernel.  PATH selects the R4 algebra; everything else is shared.
 // ============================================================================
-// Two CTAs per SM (64 registers, about 92 KB of shared memory each): a tile's two
+// Two CTAs per SM (64 registers, about 108 KB of shared memory each): a tile's two
 // look-back chains wait in one CTA while the other classifies.
 template<int PATH>
 __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
@@ -378,6 +395,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	std::uint8_t*	 g_step = g_rep + 8 * 256;							   // [8][8][8]
 	std::uint32_t*	 g_tlo	= reinterpret_cast<std::uint32_t*>(g_step + 8 * 64);  // [8][8]
 	std::uint32_t*	 g_thi	= g_tlo + 64;
+	uint4*			 g_btab = reinterpret_cast<uint4*>(smem + SmemLayout::kBtab);	// [4][256]
 
 	const int			tid	 = threadIdx.x;
 	const int			lane = tid & 31;
@@ -397,6 +415,16 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		for (int i = tid; i < 64; i += kScanThreads) {
 			g_tlo[i] = (&P->tb_lo[0][0])[i];
 			g_thi[i] = (&P->tb_hi[0][0])[i];
+		}
+		for (int i = tid; i < kByteTabDescs * 256; i += kScanThreads) {
+			const int	  d	 = i >> 8;
+			const int	  cl = (&P->rep_of[0][0])[i] & 7;
+			std::uint32_t lo = 0, hi = 0;
+			for (int st = 0; st < 4; ++st) {
+				lo |= static_cast<std::uint32_t>(P->step[d][st][cl]) << (8 * st);
+				hi |= static_cast<std::uint32_t>(P->step[d][st + 4][cl]) << (8 * st);
+			}
+			g_btab[i] = make_uint4(lo, hi, (lo & 0x07070707u) << 4, (hi & 0x07070707u) << 4);
 		}
 	}
 	if (tid == 0) {
@@ -434,7 +462,6 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	const std::uint32_t epoch	 = a.epoch & 0x3FFFFFFFu;
 	const unsigned long long doc_end = a.o + a.n;  // stream position one past the last byte
 	const unsigned long long byte_base = a.carry_in ? a.carry_in->byte_base : 0ull;
-	const bool first_chunk = byte_base == 0;
 	long long my_min_bal = 0, my_max_bal = 0, my_min_key = 0x7FFFFFFFFFFFFFFFll,
 			  my_max_key = -0x7FFFFFFFFFFFFFFFll;
 	bool any_keys = false;
@@ -508,7 +535,39 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		} else if (PATH == kPathGeneric) {
 			for (int d = 0; d < 8; ++d) gmap[d] = kIdentMap;
 			const unsigned char* wb = stage + 32 * tid;
-			for (int d = 0; d < nd; ++d) {
+			// descriptors 0..3: per-byte step tables, shuffled layout (see step_shuffled)
+			const uint4	  ident = make_uint4(0x03020100u, 0x07060504u, 0x30201000u, 0x70605040u);
+			std::uint32_t X[kByteTabDescs];
+#pragma unroll
+			for (int d = 0; d < kByteTabDescs; ++d) X[d] = kIdentMap;
+			if (lo == 0 && hi == 32) {
+#pragma unroll
+				for (int j = 0; j < 33; ++j) {	// 32 bytes and one identity step: 33 = 3 x 11
+					const uint4* row = g_btab + (j < 32 ? ((r[j >> 2] >> (8 * (j & 3))) & 0xFFu) : 0u);
+#pragma unroll
+					for (int d = 0; d < kByteTabDescs; ++d)
+						if (d < nd)
+							X[d] = step_shuffled(X[d], j < 32 ? row[d * 256] : ident);
+				}
+			} else {
+				int steps = 0;
+				for (int j = lo; j < hi; ++j, ++steps) {
+					const uint4* row = g_btab + wb[j];
+#pragma unroll
+					for (int d = 0; d < kByteTabDescs; ++d)
+						if (d < nd)
+							X[d] = step_shuffled(X[d], row[d * 256]);
+				}
+				for (; steps % 3; ++steps)
+#pragma unroll
+					for (int d = 0; d < kByteTabDescs; ++d) X[d] = step_shuffled(X[d], ident);
+			}
+#pragma unroll
+			for (int d = 0; d < kByteTabDescs; ++d)
+				if (d < nd)
+					gmap[d] = X[d];
+			// further descriptors: class tables, plain layout
+			for (int d = kByteTabDescs; d < nd; ++d) {
 				std::uint32_t m = kIdentMap;
 				for (int j = lo; j < hi; ++j) {
 					const int cl = g_rep[d * 256 + wb[j]];
@@ -687,11 +746,24 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 				const std::uint32_t pre	  = compose_map(sc.warp_maps[warp][d], gexcl[d]);
 				const std::uint32_t init  = a.carry_in ? a.carry_in->gstate[d] : P->start[d];
 				std::uint32_t		stt	  = (pre >> (4 * init)) & 0xFu;
-				for (int j = lo; j < hi; ++j) {
-					const int			cl = g_rep[d * 256 + wb[j]];
-					const std::uint32_t x  = g_step[d * 64 + stt * 8 + cl];
-					mask |= ((x >> 3) & 1u) << j;
-					stt = x & 7u;
+				if (d < kByteTabDescs && lo == 0 && hi == 32) {
+					// the byte's table row does not depend on the state: its loads run
+					// ahead, and each step is one permute (the row byte of the state)
+					const uint4* base = g_btab + d * 256;
+#pragma unroll
+					for (int j = 0; j < 32; ++j) {
+						const uint4			e = base[(r[j >> 2] >> (8 * (j & 3))) & 0xFFu];
+						const std::uint32_t x = prmt(e.x, e.y, stt);
+						mask |= ((x >> 3) & 1u) << j;
+						stt = x & 7u;
+					}
+				} else {
+					for (int j = lo; j < hi; ++j) {
+						const int			cl = g_rep[d * 256 + wb[j]];
+						const std::uint32_t x  = g_step[d * 64 + stt * 8 + cl];
+						mask |= ((x >> 3) & 1u) << j;
+						stt = x & 7u;
+					}
 				}
 				gend[d] = stt;
 			}
