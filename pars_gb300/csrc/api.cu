@@ -31,7 +31,8 @@ namespace pars {
 
 // kernels (scan_ws.cu / scan.cu / pair.cu)
 int		   scan_smem_bytes(int path);
-const void* scan_kernel(int path);
+int		   scan_variant(int n_descs);
+const void* scan_kernel(int path, int variant);
 int		   scan_ws_max_grid();
 int		   scan_ws_threads(int shape);
 int		   scan_ws_tile_bytes(int shape);
@@ -96,7 +97,7 @@ struct pars_ctx {
 	uint64_t		   arena_limit = 0;	 // 0 = unlimited
 	uint64_t		   arena_used  = 0;
 	int				   num_sms	   = 0;
-	int				   scan_blocks[5] = {0, 0, 0, 0, 0};
+	int				   scan_blocks[5] = {0, 0, 0, 0, 0};	 // general kernel, by descriptor-count variant
 	int				   fast_blocks[kWsShapes][10] = {};
 	uint64_t		   gen = 0;	 // bumped whenever a device buffer moves
 	// grid sizes and tile shapes chosen by pars_autotune / pars_tune_set:
@@ -364,17 +365,17 @@ int analyse_plan(const pars_scan_plan& p, DevPlan& h) {
 }
 
 // ---- launch helpers --------------------------------------------------------------
-int ensure_scan_config(pars_ctx* ctx, int path) {
-	if (ctx->scan_blocks[path])
+int ensure_scan_config(pars_ctx* ctx, int path, int variant) {
+	if (ctx->scan_blocks[variant])
 		return 0;
-	const void* k	  = scan_kernel(path);
+	const void* k	  = scan_kernel(path, variant);
 	const int	smem = scan_smem_bytes(path);
 	CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
 	int per_sm = 0;
 	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kScanThreads, smem));
 	if (per_sm < 1)
 		return fail(ctx, PARS_ECUDA, "scan kernel does not fit on an SM");
-	ctx->scan_blocks[path] = per_sm * ctx->num_sms;
+	ctx->scan_blocks[variant] = per_sm * ctx->num_sms;
 	return 0;
 }
 
@@ -512,7 +513,7 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 		if (int r = ensure_fast_config(ctx, s.path, br_kernel, shape))
 			return r;
 	} else {
-		if (int r = ensure_scan_config(ctx, s.path))
+		if (int r = ensure_scan_config(ctx, s.path, scan_variant(pl->host.n_descs)))
 			return r;
 	}
 	if (first)
@@ -558,8 +559,9 @@ int launch_scan(pars_ctx* ctx, const Plan* pl, const Scan& s, bool first = true)
 		CK(cudaLaunchCooperativeKernel(fast_kernel(s.path, br, shape), dim3(grid), dim3(fast_threads(s.path, shape)),
 									   wargs, fast_smem(s.path, shape), s.st));
 	} else {
-		const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[s.path]));
-		CK(cudaLaunchCooperativeKernel(scan_kernel(s.path), dim3(grid), dim3(kScanThreads), args,
+		const int v	   = scan_variant(pl->host.n_descs);
+		const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[v]));
+		CK(cudaLaunchCooperativeKernel(scan_kernel(s.path, v), dim3(grid), dim3(kScanThreads), args,
 									   scan_smem_bytes(s.path), s.st));
 	}
 	ctx->launches++;
@@ -1443,7 +1445,7 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 		if (ws) {
 			if (int r = ensure_fast_config(ctx, path, br, shape))
 				return r;
-		} else if (int r = ensure_scan_config(ctx, path)) {
+		} else if (int r = ensure_scan_config(ctx, path, scan_variant(pl->host.n_descs))) {
 			return r;
 		}
 		ScanArgs a {};
@@ -1472,9 +1474,10 @@ extern "C" int pars_scan_device_noalloc(pars_ctx* ctx, int plan_id, const uint8_
 			CK(cudaLaunchCooperativeKernel(fast_kernel(path, br, shape), dim3(grid), dim3(fast_threads(path, shape)),
 										   wargs, fast_smem(path, shape), st));
 		} else {
-			const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[path]));
+			const int v	   = scan_variant(pl->host.n_descs);
+			const int grid = static_cast<int>(std::min<uint64_t>(ntiles, ctx->scan_blocks[v]));
 			void*	  args[] = {&a};
-			CK(cudaLaunchCooperativeKernel(scan_kernel(path), dim3(grid), dim3(kScanThreads), args,
+			CK(cudaLaunchCooperativeKernel(scan_kernel(path, v), dim3(grid), dim3(kScanThreads), args,
 										   scan_smem_bytes(path), st));
 		}
 		ctx->launches++;

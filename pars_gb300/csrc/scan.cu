@@ -183,18 +183,20 @@ __device__ std::uint32_t lookback_fast(TileDesc* tiles, unsigned long long t, st
 	return excl;
 }
 
-// Chain 1 (generic maps).
+// Chain 1 (generic maps); NDL bounds the descriptor count at compile time.
+template<int NDL>
 __device__ void lookback_maps(TileDescG* tiles, unsigned long long t, std::uint32_t epoch,
 							  DevResult* res, int lane, int nd, std::uint32_t* excl, bool& fail) {
-	for (int d = 0; d < 8; ++d) excl[d] = kIdentMap;
+#pragma unroll
+	for (int d = 0; d < NDL; ++d) excl[d] = kIdentMap;
 	long long j = static_cast<long long>(t) - 1;
 	while (j >= 0) {
 		const long long idx	 = j - lane;
-		std::uint32_t	v[8];
+		std::uint32_t	v[NDL];
 		bool			incl = true;
 		bool			bad	 = false;
 #pragma unroll
-		for (int d = 0; d < 8; ++d) v[d] = kIdentMap;
+		for (int d = 0; d < NDL; ++d) v[d] = kIdentMap;
 		if (idx >= 0) {
 			const std::uint32_t s = wait_status(&tiles[idx].st1, epoch, res);
 			if (s == 0) {
@@ -212,17 +214,17 @@ __device__ void lookback_maps(TileDescG* tiles, unsigned long long t, std::uint3
 		const std::uint32_t ib	  = __ballot_sync(kFull, incl);
 		const int			first = __ffs(ib) - 1;
 		if (ib && lane > first)
-			for (int d = 0; d < 8; ++d) v[d] = kIdentMap;
+			for (int d = 0; d < NDL; ++d) v[d] = kIdentMap;
 		for (int off = 1; off < 32; off <<= 1) {
 #pragma unroll
-			for (int d = 0; d < 8; ++d) {
+			for (int d = 0; d < NDL; ++d) {
 				const std::uint32_t o = __shfl_down_sync(kFull, v[d], off);
 				if (lane + off < 32 && d < nd)
 					v[d] = compose_map(o, v[d]);
 			}
 		}
 #pragma unroll
-		for (int d = 0; d < 8; ++d) {
+		for (int d = 0; d < NDL; ++d) {
 			const std::uint32_t w = __shfl_sync(kFull, v[d], 0);
 			if (d < nd)
 				excl[d] = compose_map(w, excl[d]);
@@ -383,8 +385,11 @@ struct SmemLayout {
 // ============================================================================
 // Two CTAs per SM (64 registers, about 108 KB of shared memory each): a tile's two
 // look-back chains wait in one CTA while the other classifies.
-template<int PATH>
+// NDC: the plan's descriptor count when it is 1..4 (every descriptor loop unrolls,
+// nothing lives in local memory), 8 for any count read at run time.
+template<int PATH, int NDC>
 __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
+	constexpr int NDL = NDC;  // descriptor loop bound
 	extern __shared__ __align__(128) unsigned char smem[];
 	std::uint32_t*	 tbl	= reinterpret_cast<std::uint32_t*>(smem + SmemLayout::kTbl);
 	unsigned char*	 stages = smem + SmemLayout::kStage;
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	const DevPlan*		P	 = a.plan;
 	DevResult*			res	 = a.res;
 	const bool			brk	 = P->has_brackets != 0;
-	const int			nd	 = P->n_descs;
+	const int			nd	 = NDC < 8 ? NDC : P->n_descs;
 
 	// ---- one-time CTA set-up: replicated class table, generic tables ----------
 	for (int i = tid; i < 256 * 32; i += kScanThreads) tbl[i] = P->cls[i >> 5];
@@ -533,7 +538,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 				elem				   = aa | (bb << 1) | (qq << 2) | (dd << 3);
 			}
 		} else if (PATH == kPathGeneric) {
-			for (int d = 0; d < 8; ++d) gmap[d] = kIdentMap;
+			for (int d = 0; d < NDL; ++d) gmap[d] = kIdentMap;
 			const unsigned char* wb = stage + 32 * tid;
 			// descriptors 0..3: per-byte step tables, shuffled layout (see step_shuffled)
 			const uint4	  ident = make_uint4(0x03020100u, 0x07060504u, 0x30201000u, 0x70605040u);
@@ -594,7 +599,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 			if (lane == 31)
 				sc.warp_elem[warp] = v;
 		} else if (PATH == kPathGeneric) {
-			for (int d = 0; d < 8; ++d) {
+			for (int d = 0; d < NDL; ++d) {
 				std::uint32_t v = gmap[d];
 #pragma unroll
 				for (int off = 1; off < 32; off <<= 1) {
@@ -648,7 +653,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 			} else if (PATH == kPathGeneric) {
 				TileDescG*	  tiles = static_cast<TileDescG*>(a.tiles);
 				std::uint32_t we[8], agg[8], texcl[8];
-				for (int d = 0; d < 8; ++d) {
+				for (int d = 0; d < NDL; ++d) {
 					const std::uint32_t w = lane < 16 ? sc.warp_maps[lane][d] : kIdentMap;
 					std::uint32_t		v = w;
 #pragma unroll
@@ -667,12 +672,12 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 						for (int d = 0; d < nd; ++d) tiles[t].agg1[d] = agg[d];
 						st_release(&tiles[t].st1, (epoch << 2) | kFlagAgg);
 					}
-					lookback_maps(tiles, t, epoch, res, lane, nd, texcl, fail);
+					lookback_maps<NDL>(tiles, t, epoch, res, lane, nd, texcl, fail);
 				}
 				if (lane == 0) {
 					for (int d = 0; d < nd; ++d) tiles[t].inc1[d] = compose_map(texcl[d], agg[d]);
 					if (t == 0) {
-						for (int d = 0; d < 8; ++d)
+						for (int d = 0; d < NDL; ++d)
 							sc.init_gstate[d] = a.carry_in ? a.carry_in->gstate[d]
 														   : (d < nd ? P->start[d] : 0u);
 					}
@@ -896,7 +901,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 					if (gend[d] != P->start[d])
 						unclosed = 1;
 				if (a.carry_out)
-					for (int d = 0; d < 8; ++d) a.carry_out->gstate[d] = d < nd ? gend[d] : 0u;
+					for (int d = 0; d < NDL; ++d) a.carry_out->gstate[d] = d < nd ? gend[d] : 0u;
 			}
 			res->unclosed = unclosed;
 			if (a.carry_out)
@@ -1012,15 +1017,30 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	}
 }
 
-template __global__ void k_scan<kPathGeneric>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric, 1>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric, 2>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric, 3>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric, 4>(const ScanArgs);
+template __global__ void k_scan<kPathGeneric, 8>(const ScanArgs);
 
 int scan_smem_bytes(int path) {
 	return path == kPathGeneric ? SmemLayout::kBytesGen : SmemLayout::kBytesFast;
 }
 
-const void* scan_kernel(int path) {
+// The general kernel specialised for the plan's descriptor count (slot 0..4).
+int scan_variant(int n_descs) {
+	return n_descs >= 1 && n_descs <= 4 ? n_descs - 1 : 4;
+}
+
+const void* scan_kernel(int path, int variant) {
 	(void)path;
-	return reinterpret_cast<const void*>(&k_scan<kPathGeneric>);
+	switch (variant) {
+		case 0: return reinterpret_cast<const void*>(&k_scan<kPathGeneric, 1>);
+		case 1: return reinterpret_cast<const void*>(&k_scan<kPathGeneric, 2>);
+		case 2: return reinterpret_cast<const void*>(&k_scan<kPathGeneric, 3>);
+		case 3: return reinterpret_cast<const void*>(&k_scan<kPathGeneric, 4>);
+		default: return reinterpret_cast<const void*>(&k_scan<kPathGeneric, 8>);
+	}
 }
 
 }  // namespace pars

@@ -1,6 +1,6 @@
 """Run the scan a few times on one seeded synthetic document, for profilers.
 
-    python -m pars_gb300.profile_run <csv|json> <MiB> [repeats] [--pairs]
+    python -m pars_gb300.profile_run <csv|json|toml|clike|ini|xml> <MiB> [repeats] [--pairs]
     python -m pars_gb300.profile_run batch <documents> [repeats]
 
 Loads the plan from tests/golden/plans, generates the document with the library's
@@ -33,7 +33,12 @@ def main(argv):
         return
     with open(os.path.join(root, "tests", "golden", "plans", f"{grammar}.plan"), "rb") as f:
         plan = f.read()
-    data = synth.csv_doc(7, mib << 20) if grammar == "csv" else synth.json_doc(7, mib << 20)
+    if grammar == "csv":
+        data = synth.csv_doc(7, mib << 20)
+    elif grammar == "json":
+        data = synth.json_doc(7, mib << 20)
+    else:
+        data = synth.config_doc(grammar, 7, mib << 20)
     t = torch.from_numpy(data).cuda()
     sc = Scanner(plan)
     r = None
