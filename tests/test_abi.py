@@ -52,3 +52,40 @@ def test_null_arguments_are_rejected(L):
     assert L.pars_create(0, 0, None) == -22
     assert L.pars_destroy(None) == -22
     assert L.pars_plan_load(None, None, 0, None) == -22
+
+
+MIRRORS = {  # C struct -> its ctypes mirror in pars_gb300/_lib.py
+    "pars_device_result": "DeviceResult", "pars_host_result": "HostResult",
+    "pars_chunk_carry": "ChunkCarry", "pars_noalloc_result": "NoAllocResult",
+    "pars_batch_result": "BatchResult", "pars_server_config": "ServerConfig",
+    "pars_server_result": "ServerResult", "pars_tune_report": "TuneReport",
+}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every result / config struct of the header has the size and field offsets of
+    its ctypes mirror (compiled from the header with the host C compiler)."""
+    import shutil
+    import subprocess
+    from pars_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pars_gb300.h"', "int main(void) {"]
+    for cname, pyname in MIRRORS.items():
+        st = getattr(_lib, pyname)
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in st._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, pyname in MIRRORS.items():
+        st = getattr(_lib, pyname)
+        assert got[(cname, "size")] == ctypes.sizeof(st), cname
+        for field, _ in st._fields_:
+            assert got[(cname, field)] == getattr(st, field).offset, (cname, field)
