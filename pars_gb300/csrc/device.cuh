@@ -1,8 +1,10 @@
 // device.cuh — shared device-side definitions of the pars GB300 backend.
 //
 // Layout of the scratch the kernels share (all owned by a pars_ctx):
-//   TileDesc[]   per 16 KiB input tile: two decoupled-lookback chains
-//                (chain 1: the R4 automaton element; chain 2: R5 counts)
+//   TileDescG[]  general path, per 16 KiB input tile: two decoupled-lookback
+//                chains (chain 1: the descriptors' state maps; chain 2: R5 counts);
+//                the warp-specialised kernel keeps 64-bit self-validating
+//                aggregate words per tile instead
 //   DevResult    one per scan: counts, depth extrema, flags
 //   Counters     dynamic tile tickets and CTA-exit counters (self-resetting)
 //   key_hist     2048-bin histogram of bracket depth keys in [-1024, 1024)
@@ -26,13 +28,6 @@ constexpr std::uint32_t kFlagIncl = 2;
 // Bounded spin: after this many polls (with nanosleep back-off) a wait gives up,
 // records PARS_DEV_ERR_TIMEOUT in DevResult::error and unwinds.
 constexpr std::uint32_t kSpinLimit = 1u << 22;
-
-struct __align__(64) TileDesc {
-	std::uint32_t st1, st2;		   // chain status words
-	std::uint32_t agg1, inc1;	   // chain 1 element (fast paths)
-	std::uint64_t agg2[3];		   // chain 2: n_struct, n_open, n_close of this tile
-	std::uint64_t inc2[3];		   // chain 2 inclusive prefix
-};
 
 struct __align__(64) TileDescG {   // generic path: one nibble-packed map per descriptor
 	std::uint32_t st1, st2;

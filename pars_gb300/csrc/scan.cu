@@ -1,4 +1,7 @@
-// scan.cu — fused R1..R5 single-pass structural scan for one GB300 (sm_103a).
+// scan.cu — the general path: fused R1..R5 single-pass structural scan for any
+// plan (every descriptor kind, up to eight descriptors), one GB300 (sm_103a).  The
+// plans with a closed-form automaton run the warp-specialised kernel instead
+// (scan_ws_kernel.cuh).
 //
 // One persistent kernel streams the document through shared memory in 16 KiB
 // tiles (1-D TMA bulk copies, 3-stage mbarrier pipeline) and, per tile:
@@ -6,11 +9,9 @@
 //       shared memory (conflict-free: lane l reads column l), summing 8 lookups
 //       into one register per 8 bytes and transposing the four flag planes with
 //       byte permutes into 32-bit masks (structural, open, close, delimiter);
-//   R4  forms the automaton element of its 32-byte word (an affine map on the
-//       2-bit state (escape pending, in-string parity) for the fast paths, or a
-//       nibble-packed state map per descriptor for the generic path), scans it
-//       across the block with warp shuffles and across tiles with a decoupled
-//       look-back (chain 1);
+//   R4  forms its 32-byte word's element, a nibble-packed state map per
+//       descriptor, scans it across the block with warp shuffles and across
+//       tiles with a decoupled look-back (chain 1);
 //   R2/R3 turns the resolved state into the per-byte masked bitmap and selects
 //       structural / open / close bits outside it;
 //   R5  counts them (chain 2 look-back gives each tile its output offsets) and
@@ -33,29 +34,7 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-// ---- fast-path automaton element -------------------------------------------
-// State: bit0 e = "next byte is escaped", bit1 p = "inside a string".
-// Element (a, b, q, d) maps (e, p) -> (a&e ^ b, p ^ q ^ d&e); bits a=0 b=1 q=2 d=3.
-constexpr std::uint32_t kIdent = 1u;
-
-__device__ __forceinline__ std::uint32_t compose_fast(std::uint32_t X, std::uint32_t Y) {
-	const std::uint32_t aX = X & 1u, bX = (X >> 1) & 1u, qX = (X >> 2) & 1u, dX = (X >> 3) & 1u;
-	const std::uint32_t aY = Y & 1u, bY = (Y >> 1) & 1u, qY = (Y >> 2) & 1u, dY = (Y >> 3) & 1u;
-	return (aX & aY) | (((bX & aY) ^ bY) << 1) | ((qX ^ qY ^ (bX & dY)) << 2)
-		 | ((dX ^ (aX & dY)) << 3);
-}
-
-__device__ __forceinline__ std::uint32_t apply_fast(std::uint32_t X, std::uint32_t s) {
-	const std::uint32_t e = s & 1u, p = (s >> 1) & 1u;
-	const std::uint32_t a = X & 1u, b = (X >> 1) & 1u, q = (X >> 2) & 1u, d = (X >> 3) & 1u;
-	return ((a & e) ^ b) | ((p ^ q ^ (d & e)) << 1);
-}
-
-// ---- generic-path element: one nibble-packed map per descriptor --------------
-struct Maps {
-	std::uint32_t m[8];
-};
-
+// ---- generic-path element: one nibble-packed map per descriptor --------------// ---- generic-path element: one nibble-packed map per descriptor --------------
 constexpr std::uint32_t kIdentMap = 0x76543210u;
 
 // nibble map -> byte tables (states 0..3 in lo, 4..7 in hi)
@@ -103,12 +82,9 @@ __device__ __forceinline__ std::uint32_t compose_map(std::uint32_t X, std::uint3
 // ---- shared scratch -----------------------------------------------------------
 struct Scratch {
 	unsigned long long tile_id[kStages];
-	std::uint32_t	   warp_elem[16];
 	std::uint32_t	   warp_maps[16][8];
 	std::uint32_t	   warp_cnt[16][3];
-	std::uint32_t	   tile_excl_elem;
 	std::uint32_t	   tile_excl_maps[8];
-	std::uint32_t	   init_state;
 	std::uint32_t	   init_gstate[8];
 	unsigned long long base_cnt[3];
 	long long		   wmin_bal[16], wmax_bal[16], wmin_key[16], wmax_key[16];
@@ -141,49 +117,7 @@ __device__ __forceinline__ std::uint32_t wait_status(const std::uint32_t* st, st
 	}
 }
 
-// Chain 1 (fast element): exclusive prefix of tiles [0, t).  Executed by one warp.
-__device__ std::uint32_t lookback_fast(TileDesc* tiles, unsigned long long t, std::uint32_t epoch,
-									   DevResult* res, int lane, bool& fail) {
-	std::uint32_t excl = kIdent;
-	long long	  j	   = static_cast<long long>(t) - 1;
-	while (j >= 0) {
-		const long long idx	 = j - lane;
-		std::uint32_t	v	 = kIdent;
-		bool			incl = true;
-		bool			bad	 = false;
-		if (idx >= 0) {
-			const std::uint32_t s = wait_status(&tiles[idx].st1, epoch, res);
-			if (s == 0) {
-				bad = true;
-			} else {
-				incl = (s & 3u) == kFlagIncl;
-				v	 = incl ? ld_relaxed(&tiles[idx].inc1) : ld_relaxed(&tiles[idx].agg1);
-			}
-		}
-		if (__any_sync(kFull, bad)) {
-			fail = true;
-			return kIdent;
-		}
-		const std::uint32_t ib	  = __ballot_sync(kFull, incl);
-		const int			first = __ffs(ib) - 1;
-		if (ib && lane > first)
-			v = kIdent;
-#pragma unroll
-		for (int off = 1; off < 32; off <<= 1) {
-			const std::uint32_t o = __shfl_down_sync(kFull, v, off);
-			if (lane + off < 32)
-				v = compose_fast(o, v);
-		}
-		v	 = __shfl_sync(kFull, v, 0);
-		excl = compose_fast(v, excl);
-		if (ib)
-			break;
-		j -= 32;
-	}
-	return excl;
-}
-
-// Chain 1 (generic maps); NDL bounds the descriptor count at compile time.
+// Chain 1 (generic maps); NDL bounds the descriptor count at compile time.// Chain 1 (generic maps); NDL bounds the descriptor count at compile time.
 template<int NDL>
 __device__ void lookback_maps(TileDescG* tiles, unsigned long long t, std::uint32_t epoch,
 							  DevResult* res, int lane, int nd, std::uint32_t* excl, bool& fail) {
@@ -311,19 +245,6 @@ __device__ __forceinline__ void classify32(const std::uint32_t (&r)[8], std::uin
 	O					   = prmt(t0, t2, 0x7632);
 	C					   = prmt(t1, t3, 0x5410);
 	D					   = prmt(t1, t3, 0x7632);
-}
-
-// Exact SWAR byte-equality of 32 bytes against a replicated byte; 1 bit per byte.
-__device__ __forceinline__ std::uint32_t eq_mask32(const std::uint32_t (&r)[8], std::uint32_t rep) {
-	std::uint32_t m = 0;
-#pragma unroll
-	for (int i = 0; i < 8; ++i) {
-		const std::uint32_t t = r[i] ^ rep;
-		const std::uint32_t y = (t & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
-		const std::uint32_t z = ~(y | t) & 0x80808080u;
-		m |= ((z * 0x00204081u) >> 28) << (4 * i);
-	}
-	return m;
 }
 
 // Loads this thread's 32-byte word from the stage (the two 16-byte halves are read
@@ -462,8 +383,6 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 	__syncthreads();
 
 	const std::uint32_t tbl_lane = smem_addr(tbl) + 4u * lane;
-	const std::uint32_t escape_rep = P->escape_rep;
-	const std::uint8_t	delim	   = P->delim;
 	const std::uint32_t epoch	 = a.epoch & 0x3FFFFFFFu;
 	const unsigned long long doc_end = a.o + a.n;  // stream position one past the last byte
 	const unsigned long long byte_base = a.carry_in ? a.carry_in->byte_base : 0ull;
@@ -513,31 +432,8 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		D &= vm;
 
 		// ---- R4 (local): element of this word -----------------------------------
-		std::uint32_t elem = kIdent;
-		std::uint32_t B = 0, esc0 = 0, fbit = 0;
 		std::uint32_t gmap[8];
-		if (PATH == kPathParity || PATH == kPathDoubled) {
-			elem = 1u | ((__popc(D) & 1u) << 2);
-		} else if (PATH == kPathEscape) {
-			B							= eq_mask32(r, escape_rep) & vm;
-			const std::uint32_t runs	= B & ~(B << 1);
-			const std::uint32_t se		= runs & 0x55555555u;
-			const std::uint32_t so		= runs & 0xAAAAAAAAu;
-			const std::uint32_t ee		= (B + se) & ~B;
-			const std::uint32_t eo		= (B + so) & ~B;
-			esc0						= (ee & 0xAAAAAAAAu) | (eo & 0x55555555u);
-			const std::uint32_t nbv		= ~B & vm;
-			fbit						= nbv & (0u - nbv);	 // lowest valid non-backslash
-			if (vm != 0) {
-				const std::uint32_t bt = hi >= 32 ? B : (B << (32 - hi));
-				const std::uint32_t L  = __clz(~bt);
-				const std::uint32_t aa = nbv == 0 ? 1u : 0u;
-				const std::uint32_t bb = L & 1u;
-				const std::uint32_t qq = __popc(D & ~esc0) & 1u;
-				const std::uint32_t dd = (D & fbit) ? 1u : 0u;
-				elem				   = aa | (bb << 1) | (qq << 2) | (dd << 3);
-			}
-		} else if (PATH == kPathGeneric) {
+		{
 			for (int d = 0; d < NDL; ++d) gmap[d] = kIdentMap;
 			const unsigned char* wb = stage + 32 * tid;
 			// descriptors 0..3: per-byte step tables, shuffled layout (see step_shuffled)
@@ -583,22 +479,8 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		}
 
 		// ---- chain 1: block scan + look-back ---------------------------------------
-		std::uint32_t excl_elem = kIdent;  // thread's exclusive element within the tile
 		std::uint32_t gexcl[8];
-		if (PATH != kPathNone && PATH != kPathGeneric) {
-			std::uint32_t v = elem;
-#pragma unroll
-			for (int off = 1; off < 32; off <<= 1) {
-				const std::uint32_t o = __shfl_up_sync(kFull, v, off);
-				if (lane >= off)
-					v = compose_fast(o, v);
-			}
-			excl_elem = __shfl_up_sync(kFull, v, 1);
-			if (lane == 0)
-				excl_elem = kIdent;
-			if (lane == 31)
-				sc.warp_elem[warp] = v;
-		} else if (PATH == kPathGeneric) {
+		{
 			for (int d = 0; d < NDL; ++d) {
 				std::uint32_t v = gmap[d];
 #pragma unroll
@@ -616,41 +498,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		__syncthreads();
 		if (warp == 0) {
 			bool fail = false;
-			if (PATH != kPathNone && PATH != kPathGeneric) {
-				// warp-exclusive prefix of the 16 warp aggregates
-				std::uint32_t w = lane < 16 ? sc.warp_elem[lane] : kIdent;
-				std::uint32_t v = w;
-#pragma unroll
-				for (int off = 1; off < 16; off <<= 1) {
-					const std::uint32_t o = __shfl_up_sync(kFull, v, off);
-					if (lane >= off)
-						v = compose_fast(o, v);
-				}
-				const std::uint32_t agg = __shfl_sync(kFull, v, 15);
-				std::uint32_t		we	= __shfl_up_sync(kFull, v, 1);
-				if (lane == 0)
-					we = kIdent;
-				TileDesc* tiles = static_cast<TileDesc*>(a.tiles);
-				std::uint32_t texcl = kIdent;
-				if (t > 0) {
-					if (lane == 0) {
-						tiles[t].agg1 = agg;
-						st_release(&tiles[t].st1, (epoch << 2) | kFlagAgg);
-					}
-					texcl = lookback_fast(tiles, t, epoch, res, lane, fail);
-				}
-				if (lane == 0) {
-					if (t == 0)
-						sc.init_state = a.carry_in ? a.carry_in->fstate : 0u;
-					tiles[t].inc1 = compose_fast(texcl, agg);
-
-				}
-				__syncwarp();
-				if (lane == 0)
-					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
-				if (lane < 16)
-					sc.warp_elem[lane] = compose_fast(texcl, we);	// tile-exclusive per warp
-			} else if (PATH == kPathGeneric) {
+			{
 				TileDescG*	  tiles = static_cast<TileDescG*>(a.tiles);
 				std::uint32_t we[8], agg[8], texcl[8];
 				for (int d = 0; d < NDL; ++d) {
@@ -687,8 +535,6 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 					st_release(&tiles[t].st1, (epoch << 2) | kFlagIncl);
 				if (lane < 16)
 					for (int d = 0; d < nd; ++d) sc.warp_maps[lane][d] = compose_map(texcl[d], we[d]);
-			} else {  // kPathNone: still publish so the structure is uniform
-
 			}
 			if (fail && lane == 0)
 				sc.failed = 1;
@@ -698,54 +544,9 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 			break;
 
 		// ---- R4 (resolve) + R3: per-byte masked bitmap ---------------------------
-		std::uint32_t mask = 0, endstate = 0, last_flag = 0;
+		std::uint32_t mask = 0;
 		std::uint32_t gend[8];
-		if (PATH == kPathParity || PATH == kPathDoubled || PATH == kPathEscape) {
-			// state at this word's first byte
-			const std::uint32_t pre = compose_fast(sc.warp_elem[warp], excl_elem);
-			// tile 0 publishes init via smem; other tiles read carry directly
-			const std::uint32_t init = a.carry_in ? a.carry_in->fstate : 0u;
-			const std::uint32_t st	 = apply_fast(pre, init);
-			const std::uint32_t e_in = st & 1u, p_in = (st >> 1) & 1u;
-			std::uint32_t		tog = D;
-			std::uint32_t		esc = 0;
-			if (PATH == kPathEscape) {
-				esc = esc0 ^ (e_in ? fbit : 0u);
-				tog = D & ~esc;
-			}
-			const std::uint32_t incl = prefix_xor32(tog);
-			std::uint32_t		ex	 = incl ^ tog;
-			if (p_in)
-				ex = ~ex;
-			mask = ex & vm;
-			if (PATH == kPathDoubled) {
-				// Was the byte before each byte a delimiter?  Inside the word that is
-				// D << 1; the byte before bit `lo` comes from the previous word, the
-				// previous tile, or (at the document/chunk start) the carry.
-				std::uint32_t prev = __shfl_up_sync(kFull, D >> 31, 1);
-				const bool	  first = (q0 + lo == a.o);	 // word holds the first byte
-				if (first) {
-					prev = a.carry_in ? (a.carry_in->last_delim & 1u) : 0u;
-				} else if (lane == 0 && vm != 0) {
-					// lo == 0 and q0 > o here: the previous byte is a document byte
-					prev = (tid > 0 ? stage[32 * tid - 1] : a.base[q0 - 1]) == delim ? 1u : 0u;
-				}
-				const std::uint32_t dprev = (D << 1) | ((prev & 1u) << lo);
-				mask |= D & dprev;
-				mask &= vm;
-			}
-			if (PATH == kPathEscape) {
-				if (D & esc & ~mask & vm)
-					atomicOr(&res->spec_fail, 1u);
-			}
-			if (hi > lo && doc_end <= q0 + 32 && doc_end > q0) {
-				// this word holds the last byte of the document/chunk
-				endstate				  = apply_fast(elem, st);
-				const std::uint32_t lastb = 1u << (hi - 1);
-				last_flag				  = (PATH == kPathEscape) ? ((tog & lastb) ? 1u : 0u)
-																  : ((D & lastb) ? 1u : 0u);
-			}
-		} else if (PATH == kPathGeneric) {
+		{
 			const unsigned char* wb = stage + 32 * tid;
 			for (int d = 0; d < nd; ++d) {
 				const std::uint32_t pre	  = compose_map(sc.warp_maps[warp][d], gexcl[d]);
@@ -821,25 +622,8 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 											   __shfl_sync(kFull, v2, 15)};
 			unsigned long long base[3]	  = {0, 0, 0};
 			bool			   fail		  = false;
-			if (PATH == kPathGeneric) {
+			{
 				TileDescG* tiles = static_cast<TileDescG*>(a.tiles);
-				if (t > 0) {
-					if (lane == 0) {
-						for (int k = 0; k < 3; ++k) tiles[t].agg2[k] = tot[k];
-						st_release(&tiles[t].st2, (epoch << 2) | kFlagAgg);
-					}
-					lookback_counts(tiles, t, epoch, res, lane, base, fail);
-				} else if (a.carry_in) {
-					base[0] = a.carry_in->ns;
-					base[1] = a.carry_in->no;
-					base[2] = a.carry_in->nc;
-				}
-				if (lane == 0) {
-					for (int k = 0; k < 3; ++k) tiles[t].inc2[k] = base[k] + tot[k];
-					st_release(&tiles[t].st2, (epoch << 2) | kFlagIncl);
-				}
-			} else {
-				TileDesc* tiles = static_cast<TileDesc*>(a.tiles);
 				if (t > 0) {
 					if (lane == 0) {
 						for (int k = 0; k < 3; ++k) tiles[t].agg2[k] = tot[k];
@@ -889,14 +673,7 @@ __global__ void __launch_bounds__(kScanThreads, 2) k_scan(const ScanArgs a) {
 		// ---- end-of-document state (the thread holding the last byte) -----------
 		if (hi > lo && doc_end <= q0 + 32 && doc_end > q0) {
 			std::uint32_t unclosed = 0;
-			if (PATH == kPathParity || PATH == kPathDoubled || PATH == kPathEscape) {
-				unclosed = ((endstate >> 1) & 1u) | last_flag;
-				if (a.carry_out) {
-					a.carry_out->fstate		 = endstate;
-					a.carry_out->last_delim	 = (D >> (hi - 1)) & 1u;
-					a.carry_out->last_toggle = last_flag;
-				}
-			} else if (PATH == kPathGeneric) {
+			{
 				for (int d = 0; d < nd; ++d)
 					if (gend[d] != P->start[d])
 						unclosed = 1;
