@@ -23,6 +23,7 @@ the data path; value = all ranks' bytes / max rank time.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import os
 import statistics
@@ -335,27 +336,35 @@ def serving_leg(args, seconds=0.6, loads=(0.1, 0.5, 0.9, 1.2)):
         r = np.random.default_rng(seed)
         picks = r.integers(0, len(pool), n_req)
         gaps = r.exponential(1.0 / rate, n_req) if rate else np.zeros(n_req)
-        tickets, nbytes = [], 0
-        t0 = time.perf_counter()
-        due = t0
-        for i in range(n_req):
-            due += gaps[i]
-            while True:
-                left = due - time.perf_counter()
-                if left <= 0:
-                    break
-                if left > 2e-4:
-                    time.sleep(left - 1e-4)
-            g, t = pool[picks[i]]
-            tickets.append(srv.submit(plans[g], t.data_ptr(), t.numel()))
-            nbytes += t.numel()
+        pending, nbytes = collections.deque(), 0
         lat, folded, first, last = [], 0, None, 0
-        for tk in tickets:
+
+        def consume(tk):  # a client takes its result and releases it
+            nonlocal folded, first, last
             res = srv.wait(tk, copy=False)
             lat.append(res["latency_ns"] / 1e6)
             folded += res["batch_docs"]
             first = res["submit_ns"] if first is None else min(first, res["submit_ns"])
             last = max(last, res["done_ns"])
+
+        t0 = time.perf_counter()
+        due = t0
+        for i in range(n_req):
+            due += gaps[i]
+            while True:
+                # results that are done are consumed while waiting for the next arrival
+                while pending and srv.done(pending[0]):
+                    consume(pending.popleft())
+                left = due - time.perf_counter()
+                if left <= 0:
+                    break
+                if left > 2e-4:
+                    time.sleep(min(left - 1e-4, 1e-3))
+            g, t = pool[picks[i]]
+            pending.append(srv.submit(plans[g], t.data_ptr(), t.numel()))
+            nbytes += t.numel()
+        while pending:
+            consume(pending.popleft())
         wall = (last - first) / 1e9	 # the server's clock: first submission to last completion
         lat = np.array(lat)
         return {"requests": n_req, "GBps": round(nbytes / wall / 1e9, 3),

@@ -231,7 +231,9 @@ typedef struct pars_server_config {
   uint32_t workers;              /* launches in flight (0: 2)                         */
   uint64_t arena_bytes;          /* device memory for admitted inputs                 */
   uint32_t max_batch_docs;       /* requests folded into one launch (1: plain path)   */
-  uint32_t reserved;
+  uint32_t result_mib;           /* pinned host memory results are copied into, MiB
+                                    (0: 1024); a result that does not fit goes to the
+                                    request's own pageable buffers                    */
 } pars_server_config;
 
 typedef struct pars_server_result {

@@ -22,6 +22,8 @@ ERRORS = {
     -110: "PARS_ETIMEDOUT", -34: "PARS_ERANGE", -16: "PARS_EBUSY", -11: "PARS_EAGAIN",
 }
 
+PARS_EAGAIN = -11  # pars_server_poll: the request is not finished yet
+
 PLAN_BYTES = 3177
 
 u8p = ctypes.POINTER(ctypes.c_uint8)
@@ -86,7 +88,7 @@ class BatchResult(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("workers", ctypes.c_uint32),
                 ("arena_bytes", ctypes.c_uint64), ("max_batch_docs", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("result_mib", ctypes.c_uint32)]
 
 
 class ServerResult(ctypes.Structure):

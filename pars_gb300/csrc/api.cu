@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <functional>
 #include <numeric>
 #include <queue>
@@ -166,6 +167,9 @@ struct pars_ctx {
 			uint64_t		launches;
 		};
 		std::vector<GraphEntry> graphs;
+		// layouts seen recently: a layout is captured the second time it runs, so
+		// one-off layouts (a serving loop's batches) never pay for a capture
+		std::vector<std::array<uint64_t, 12>> seen;
 	} batch;
 };
 
@@ -1874,12 +1878,20 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		CK(cudaMemcpyAsync(B.h_res, ctx->res, sizeof(DevResult), cudaMemcpyDeviceToHost, st));
 		return 0;
 		};
-		// Replay a captured graph of this layout, or capture one (a capturable stream:
-		// not the legacy default stream).
+		// Replay a captured graph of this layout, or capture one when the layout
+		// repeats (a capturable stream: not the legacy default stream).
 		const uint64_t key[12] = {reinterpret_cast<uintptr_t>(pl), static_cast<uint64_t>(path), br ? 1u : 0u, flags,
 								  static_cast<uint64_t>(G), ndocs, cap_s, cap_b, ctx->gen,
 								  reinterpret_cast<uintptr_t>(B.h_pin), reinterpret_cast<uintptr_t>(base), total};
 		bool done = false;
+		std::array<uint64_t, 12> akey;
+		std::memcpy(akey.data(), key, sizeof key);
+		const bool repeat = std::find(B.seen.begin(), B.seen.end(), akey) != B.seen.end();
+		if (!repeat) {
+			if (B.seen.size() >= 16)
+				B.seen.erase(B.seen.begin());
+			B.seen.push_back(akey);
+		}
 		if (st != nullptr) {
 			for (auto& g : B.graphs)
 				if (std::memcmp(g.key, key, sizeof key) == 0) {
@@ -1888,7 +1900,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 					done = true;
 					break;
 				}
-			if (!done) {
+			if (!done && repeat) {
 				CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
 				const int	rc = launch_all(true);
 				cudaGraph_t graph = nullptr;

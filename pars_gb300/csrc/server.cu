@@ -10,7 +10,10 @@
 // uploading the requests that arrived meanwhile: their work overlaps on the device.
 // A launch of a single request (always, with max_batch_docs = 1: the plain
 // per-request path the batched path is measured against) is one pars_scan_device.
-// Results come back through the worker's pinned staging.
+// Results land in a server-wide pool of pinned host memory: each request's offsets
+// (and pairs) are copied from the device straight into its own slice, which the
+// client reads in place until it releases the request.  A result the pool cannot
+// hold goes through the worker's pinned staging into the request's own buffers.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -18,6 +21,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -28,6 +32,9 @@
 #include "pars_gb300.h"
 
 namespace {
+
+// Requests from this size up run alone (the single-document launch).
+constexpr std::uint64_t kServeSoloBytes = 1ull << 20;
 
 std::uint64_t now_ns() {
 	return static_cast<std::uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -44,9 +51,74 @@ struct Request {
 	std::uint64_t		   submit_ns = 0, start_ns = 0, done_ns = 0;
 	std::uint32_t		   batch_docs = 0;
 	int					   status = PARS_EAGAIN;
-	std::vector<std::uint32_t> structural;
+	std::vector<std::uint32_t> structural;	 // when the result is not in the pool
 	std::vector<std::int32_t>  pair_pos;
+	std::uint32_t*		   pooled = nullptr;  // in the pool: offsets, then pairs
+	std::size_t			   pooled_bytes = 0;
+	std::uint64_t		   n_struct = 0;
+	bool				   has_pairs = false;
 	std::int32_t		   balanced = 1, well_formed = 1, max_depth = 0, unclosed = 0;
+};
+
+// Pinned host memory for results: first fit over a free list of (offset, size),
+// neighbours merged on release.  Thread-safe.
+class ResultPool {
+  public:
+	int init(std::size_t bytes) {
+		if (cudaHostAlloc(reinterpret_cast<void**>(&base_), bytes, cudaHostAllocDefault) != cudaSuccess) {
+			cudaGetLastError();
+			base_ = nullptr;
+			return PARS_ENOMEM;
+		}
+		cap_ = bytes;
+		free_.emplace(0, bytes);
+		return 0;
+	}
+	void destroy() {
+		if (base_)
+			cudaFreeHost(base_);
+		base_ = nullptr;
+	}
+	void* alloc(std::size_t bytes) {
+		bytes = (bytes + 255) & ~std::size_t(255);
+		std::lock_guard<std::mutex> lk(mu_);
+		for (auto it = free_.begin(); it != free_.end(); ++it) {
+			if (it->second < bytes)
+				continue;
+			const std::size_t off = it->first, left = it->second - bytes;
+			free_.erase(it);
+			if (left)
+				free_.emplace(off + bytes, left);
+			return base_ + off;
+		}
+		return nullptr;
+	}
+	void release(void* p, std::size_t bytes) {
+		if (!p)
+			return;
+		bytes = (bytes + 255) & ~std::size_t(255);
+		std::lock_guard<std::mutex> lk(mu_);
+		std::size_t off = static_cast<std::uint8_t*>(p) - base_;
+		auto		nx	= free_.lower_bound(off);
+		if (nx != free_.end() && off + bytes == nx->first) {  // merge with the next block
+			bytes += nx->second;
+			nx = free_.erase(nx);
+		}
+		if (nx != free_.begin()) {	// merge with the previous block
+			auto pv = std::prev(nx);
+			if (pv->first + pv->second == off) {
+				pv->second += bytes;
+				return;
+			}
+		}
+		free_.emplace(off, bytes);
+	}
+
+  private:
+	std::mutex						   mu_;
+	std::uint8_t*					   base_ = nullptr;
+	std::size_t						   cap_	 = 0;
+	std::map<std::size_t, std::size_t> free_;
 };
 
 struct Worker {
@@ -74,6 +146,7 @@ struct pars_server {
 	std::uint64_t					  next_ticket = 1;
 	bool							  stop		  = false;
 	std::string						  err;
+	ResultPool						  pool;
 };
 
 namespace {
@@ -92,6 +165,19 @@ int grow_pinned(Worker& w, std::size_t words) {
 	}
 	w.h_cap = want;
 	return 0;
+}
+
+// A pool slice of `words` 32-bit words for request q's results, or null when the
+// pool cannot hold them (the caller stages them instead).
+std::uint32_t* take_pooled(pars_server* s, Request& q, std::size_t words) {
+	if (words == 0)
+		return nullptr;
+	void* p = s->pool.alloc(words * 4);
+	if (p) {
+		q.pooled	   = static_cast<std::uint32_t*>(p);
+		q.pooled_bytes = words * 4;
+	}
+	return static_cast<std::uint32_t*>(p);
 }
 
 // Runs one launch over `batch` (all of one plan) on worker `w`; fills the requests.
@@ -118,21 +204,31 @@ void run_batch(pars_server* s, Worker& w, std::vector<std::shared_ptr<Request>>&
 		const int rc = pars_scan_device(w.ctx, plan, w.d_in, batch[0]->n, flags, w.stream, &r);
 		if (rc)
 			return fail_all(rc);
-		auto& q = *batch[0];
-		if (grow_pinned(w, r.n_struct * (pairs ? 2 : 1)))
-			return fail_all(PARS_ENOMEM);
+		auto&			  q		= *batch[0];
+		const bool		  wantp = pairs && r.pair_pos;
+		const std::size_t words = r.n_struct * (wantp ? 2 : 1);
+		q.n_struct				= r.n_struct;
+		q.has_pairs				= wantp;
+		std::uint32_t* dst		= take_pooled(s, q, words);
+		if (!dst) {
+			if (grow_pinned(w, words))
+				return fail_all(PARS_ENOMEM);
+			dst = w.h_u32;
+		}
 		if (r.n_struct)
-			cudaMemcpyAsync(w.h_u32, r.structural, r.n_struct * 4, cudaMemcpyDeviceToHost, w.stream);
-		if (pairs && r.pair_pos && r.n_struct)
-			cudaMemcpyAsync(w.h_u32 + r.n_struct, r.pair_pos, r.n_struct * 4, cudaMemcpyDeviceToHost, w.stream);
+			cudaMemcpyAsync(dst, r.structural, r.n_struct * 4, cudaMemcpyDeviceToHost, w.stream);
+		if (wantp && r.n_struct)
+			cudaMemcpyAsync(dst + r.n_struct, r.pair_pos, r.n_struct * 4, cudaMemcpyDeviceToHost, w.stream);
 		if (cudaStreamSynchronize(w.stream) != cudaSuccess) {
 			cudaGetLastError();
 			return fail_all(PARS_ECUDA);
 		}
-		q.structural.assign(w.h_u32, w.h_u32 + r.n_struct);
-		if (pairs && r.pair_pos)
-			q.pair_pos.assign(reinterpret_cast<const std::int32_t*>(w.h_u32) + r.n_struct,
-							  reinterpret_cast<const std::int32_t*>(w.h_u32) + 2 * r.n_struct);
+		if (!q.pooled) {
+			q.structural.assign(dst, dst + r.n_struct);
+			if (wantp)
+				q.pair_pos.assign(reinterpret_cast<const std::int32_t*>(dst) + r.n_struct,
+								  reinterpret_cast<const std::int32_t*>(dst) + 2 * r.n_struct);
+		}
 		q.balanced	  = r.balanced;
 		q.well_formed = r.well_formed;
 		q.max_depth	  = r.max_depth;
@@ -158,34 +254,48 @@ void run_batch(pars_server* s, Worker& w, std::vector<std::shared_ptr<Request>>&
 		return fail_all(PARS_ECUDA);
 	}
 	std::vector<std::uint32_t> rec(w.h_u32, w.h_u32 + static_cast<std::size_t>(nd) * 6);
-	// every request's offsets (and pairs) back to back through the pinned staging
-	std::size_t words = 0;
-	for (std::uint32_t i = 0; i < nd; ++i) words += static_cast<std::size_t>(rec[nd + i]) * (pairs ? 2 : 1);
+	// every request's offsets (and pairs) into its pool slice, or back to back
+	// through the pinned staging when the pool cannot hold it
+	const bool				   wantp = pairs && br.pair_pos;
+	std::vector<std::uint32_t*> dst(nd, nullptr);
+	std::size_t				   words = 0;
+	for (std::uint32_t i = 0; i < nd; ++i) {
+		auto&			  q	 = *batch[i];
+		const std::size_t ws = static_cast<std::size_t>(rec[nd + i]) * (wantp ? 2 : 1);
+		q.n_struct			 = rec[nd + i];
+		q.has_pairs			 = wantp;
+		dst[i]				 = take_pooled(s, q, ws);
+		if (!dst[i])
+			words += ws;
+	}
 	if (grow_pinned(w, words))
 		return fail_all(PARS_ENOMEM);
 	std::size_t at = 0;
 	for (std::uint32_t i = 0; i < nd; ++i) {
 		const std::uint32_t so = rec[i], ns = rec[nd + i];
-		if (ns) {
-			cudaMemcpyAsync(w.h_u32 + at, br.structural + so, ns * 4ull, cudaMemcpyDeviceToHost, w.stream);
-			if (pairs && br.pair_pos)
-				cudaMemcpyAsync(w.h_u32 + at + ns, br.pair_pos + so, ns * 4ull, cudaMemcpyDeviceToHost, w.stream);
+		if (!dst[i]) {
+			dst[i] = w.h_u32 + at;
+			at += static_cast<std::size_t>(ns) * (wantp ? 2 : 1);
 		}
-		at += static_cast<std::size_t>(ns) * (pairs ? 2 : 1);
+		if (ns) {
+			cudaMemcpyAsync(dst[i], br.structural + so, ns * 4ull, cudaMemcpyDeviceToHost, w.stream);
+			if (wantp)
+				cudaMemcpyAsync(dst[i] + ns, br.pair_pos + so, ns * 4ull, cudaMemcpyDeviceToHost, w.stream);
+		}
 	}
 	if (cudaStreamSynchronize(w.stream) != cudaSuccess) {
 		cudaGetLastError();
 		return fail_all(PARS_ECUDA);
 	}
-	at = 0;
 	for (std::uint32_t i = 0; i < nd; ++i) {
 		auto&				q  = *batch[i];
 		const std::uint32_t ns = rec[nd + i];
-		q.structural.assign(w.h_u32 + at, w.h_u32 + at + ns);
-		if (pairs && br.pair_pos)
-			q.pair_pos.assign(reinterpret_cast<const std::int32_t*>(w.h_u32) + at + ns,
-							  reinterpret_cast<const std::int32_t*>(w.h_u32) + at + 2 * ns);
-		at += static_cast<std::size_t>(ns) * (pairs ? 2 : 1);
+		if (!q.pooled) {
+			q.structural.assign(dst[i], dst[i] + ns);
+			if (wantp)
+				q.pair_pos.assign(reinterpret_cast<const std::int32_t*>(dst[i]) + ns,
+								  reinterpret_cast<const std::int32_t*>(dst[i]) + 2 * ns);
+		}
 		q.unclosed	  = static_cast<std::int32_t>(rec[2 * nd + i]);
 		q.balanced	  = br.balanced ? static_cast<std::int32_t>(rec[3 * nd + i]) : 1;
 		q.well_formed = br.well_formed ? static_cast<std::int32_t>(rec[4 * nd + i]) : 1;
@@ -204,13 +314,17 @@ void worker_loop(pars_server* s, Worker* w) {
 			if (s->stop)
 				return;
 			// admission: the oldest request's plan, then every pending request of that
-			// plan that fits the free room of this worker's arena slice
+			// plan that fits the free room of this worker's arena slice.  A large
+			// request runs alone on the whole grid (in a batch launch a document
+			// stays on one CTA, and every request of the batch would wait for it);
+			// large requests are never folded into a batch of small ones.
 			const int	  plan	= s->pending.front()->plan;
 			std::uint64_t room	= w->cap;
-			const std::uint32_t maxd = s->cfg.max_batch_docs ? s->cfg.max_batch_docs : 1;
+			const bool	  solo	= s->pending.front()->n >= kServeSoloBytes;
+			const std::uint32_t maxd = solo ? 1u : (s->cfg.max_batch_docs ? s->cfg.max_batch_docs : 1);
 			for (auto it = s->pending.begin(); it != s->pending.end() && batch.size() < maxd;) {
 				auto& r = *it;
-				if (r->plan == plan && (r->n <= room || batch.empty())) {
+				if (r->plan == plan && (r->n <= room || batch.empty()) && (batch.empty() || r->n < kServeSoloBytes)) {
 					if (r->n > w->cap) {
 						// never fits: fail it rather than block the queue
 						r->status  = PARS_ERANGE;
@@ -246,10 +360,15 @@ void worker_loop(pars_server* s, Worker* w) {
 
 void fill(const Request& r, pars_server_result* out) {
 	std::memset(out, 0, sizeof *out);
-	out->status		   = r.status;
-	out->structural	   = r.structural.data();
-	out->pair_pos	   = r.pair_pos.empty() ? nullptr : r.pair_pos.data();
-	out->n_struct	   = r.structural.size();
+	out->status = r.status;
+	if (r.pooled) {
+		out->structural = r.pooled;
+		out->pair_pos	= r.has_pairs ? reinterpret_cast<const std::int32_t*>(r.pooled) + r.n_struct : nullptr;
+	} else {
+		out->structural = r.structural.data();
+		out->pair_pos	= r.pair_pos.empty() ? nullptr : r.pair_pos.data();
+	}
+	out->n_struct = r.status == 0 ? r.n_struct : 0;
 	out->balanced	   = r.balanced;
 	out->well_formed   = r.well_formed;
 	out->max_depth	   = r.max_depth;
@@ -289,6 +408,8 @@ int pars_server_create(const pars_server_config* cfg, pars_server** out) {
 		w->cap = slice;
 		s->workers.push_back(std::move(w));
 	}
+	// results in pinned memory; without it every result is staged and copied
+	s->pool.init(static_cast<std::size_t>(cfg->result_mib ? cfg->result_mib : 1024u) << 20);
 	for (auto& w : s->workers) w->thread = std::thread(worker_loop, s, w.get());
 	*out = s;
 	return 0;
@@ -318,6 +439,7 @@ int pars_server_destroy(pars_server* s) {
 		if (w->ctx)
 			pars_destroy(w->ctx);
 	}
+	s->pool.destroy();
 	delete s;
 	return 0;
 }
@@ -395,6 +517,8 @@ int pars_server_release(pars_server* s, uint64_t ticket) {
 	auto it = s->all.find(ticket);
 	if (it == s->all.end() || it->second->done_ns == 0)
 		return PARS_EINVAL;
+	s->pool.release(it->second->pooled, it->second->pooled_bytes);
+	it->second->pooled = nullptr;
 	s->all.erase(it);
 	return 0;
 }

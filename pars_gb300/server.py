@@ -10,11 +10,12 @@ from ._lib import PARS_WANT_PAIRS, ParsError, lib
 class Server:
     """Requests of any loaded plan are queued, admitted by free arena memory into a
     worker's launch (up to max_batch_docs per launch; 1 = the plain per-request
-    path) and answered with host copies of their results."""
+    path) and answered with host copies of their results (in a pool of pinned
+    memory of result_mib MiB, 0 = 1024, while it has room)."""
 
     def __init__(self, device: int = 0, arena_bytes: int = 8 << 30, workers: int = 2,
-                 max_batch_docs: int = 4096):
-        cfg = _lib.ServerConfig(device, workers, arena_bytes, max_batch_docs, 0)
+                 max_batch_docs: int = 4096, result_mib: int = 0):
+        cfg = _lib.ServerConfig(device, workers, arena_bytes, max_batch_docs, result_mib)
         h = ctypes.c_void_p()
         rc = lib().pars_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc:
@@ -48,6 +49,16 @@ class Server:
         if rc:
             raise ParsError(rc, "pars_server_submit")
         return t.value
+
+    def done(self, ticket: int) -> bool:
+        """Whether the request has finished (pars_server_poll; does not block)."""
+        r = _lib.ServerResult()
+        rc = lib().pars_server_poll(self.handle, ticket, ctypes.byref(r))
+        if rc == _lib.PARS_EAGAIN:
+            return False
+        if rc:
+            raise ParsError(rc, "pars_server_poll")
+        return True
 
     def wait(self, ticket: int, release: bool = True, copy: bool = True) -> dict:
         """Blocks until the request is done; with copy=False only its record (no

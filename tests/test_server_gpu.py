@@ -24,9 +24,11 @@ def make_requests(seed, n):
     return reqs
 
 
-@pytest.mark.parametrize("max_batch_docs", [4096, 1])
-def test_server_results_equal_single_scans(max_batch_docs):
-    srv = Server(arena_bytes=1 << 30, workers=2, max_batch_docs=max_batch_docs)
+@pytest.mark.parametrize("max_batch_docs,result_mib", [(4096, 0), (1, 0), (4096, 1), (1, 1)])
+def test_server_results_equal_single_scans(max_batch_docs, result_mib):
+    """With the default pinned result pool every result lands in it; with a 1 MiB
+    pool most do not fit and go through staging into the request's own buffers."""
+    srv = Server(arena_bytes=1 << 30, workers=2, max_batch_docs=max_batch_docs, result_mib=result_mib)
     plans = {g: srv.load_plan(plan_bytes(g)) for g in ("json", "csv")}
     reqs = make_requests(11, 120)
     tickets = [srv.submit(plans[g], t.data_ptr(), t.numel(), want_pairs=True) for g, t in reqs]
