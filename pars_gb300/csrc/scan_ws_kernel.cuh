@@ -817,16 +817,16 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 					if (!interior)
 						Bk &= vm;
 					F.dd[h]					  = Bk;	 // the escape path keeps its backslashes here
-					const EscWord		W	  = esc_word(Bk, D, vm);
-					const std::uint32_t above = W.fbit ? ~((W.fbit << 1) - 1u) : 0u;
-					const std::uint32_t in0 = above & ~W.ex0, in1 = above & W.ex0;
+					const EscWord		ew	  = esc_word(Bk, D, vm);
+					const std::uint32_t above = ew.fbit ? ~((ew.fbit << 1) - 1u) : 0u;
+					const std::uint32_t in0 = above & ~ew.ex0, in1 = above & ew.ex0;
 					ex0[h]					= 0;
 					e[0]					= __popc(S & in0) | (__popc(S & in1) << 16);
 					e[1]					= BR ? (__popc(O & in0) | (__popc(O & in1) << 16)) : 0u;
 					e[2]					= BR ? (__popc(C & in0) | (__popc(C & in1) << 16)) : 0u;
-					const std::uint32_t fcl = ((S & W.fbit) ? 1u : 0u) | ((O & W.fbit) ? 2u : 0u)
-											| ((C & W.fbit) ? 4u : 0u);
-					e[3] = W.elem | ((BR ? fcl : (fcl & 1u)) << 4);
+					const std::uint32_t fcl = ((S & ew.fbit) ? 1u : 0u) | ((O & ew.fbit) ? 2u : 0u)
+											| ((C & ew.fbit) ? 4u : 0u);
+					e[3] = ew.elem | ((BR ? fcl : (fcl & 1u)) << 4);
 				} else {
 					ex0[h] = prefix_xor32(D) ^ D;
 					e[0]   = 0;
@@ -1014,13 +1014,13 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 					std::uint32_t			 mask = 0, esc = 0, welem = 0;
 					if (PATH == kPathEscape) {
 						// the word's exact entry state resolves the first byte's escape
-						const EscWord		W	  = esc_word(F.dd[h], F.D[h], vm);
+						const EscWord		ew	  = esc_word(F.dd[h], F.D[h], vm);
 						const std::uint32_t e_w	  = s_w & 1u, pw = (s_w >> 1) & 1u;
-						const std::uint32_t above = W.fbit ? ~((W.fbit << 1) - 1u) : 0u;
-						const std::uint32_t exw	  = W.ex0 ^ ((e_w && (F.D[h] & W.fbit)) ? above : 0u);
+						const std::uint32_t above = ew.fbit ? ~((ew.fbit << 1) - 1u) : 0u;
+						const std::uint32_t exw	  = ew.ex0 ^ ((e_w && (F.D[h] & ew.fbit)) ? above : 0u);
 						mask					  = (exw ^ (pw ? 0xFFFFFFFFu : 0u)) & vm;
-						esc						  = W.esc0 ^ (e_w ? W.fbit : 0u);
-						welem					  = W.elem;
+						esc						  = ew.esc0 ^ (e_w ? ew.fbit : 0u);
+						welem					  = ew.elem;
 						// an escaped quote outside a string: the descriptor would toggle there
 						// (a backslash outside strings is inert); the host reruns this input
 						// on the general kernel
