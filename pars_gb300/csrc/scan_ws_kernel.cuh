@@ -1088,14 +1088,15 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 				if (total <= static_cast<std::uint32_t>(kListCap)) {
 					std::uint16_t* L = list_all + warp * kListCap;
 					std::uint32_t  o = incl - cnt;
-#pragma unroll
-					for (int h = 0; h < 2; ++h) {
-						std::uint32_t m = sel[h];
+					{
+						// one loop over both words, codes lane << 6 | bit (bit 32+ = word 1);
+						// the rounds fetch the bracket planes from the code's lane
+						unsigned long long	m  = sel[0] | (static_cast<unsigned long long>(sel[1]) << 32);
+						const std::uint32_t lb = static_cast<std::uint32_t>(lane) << 6;
 						while (m) {
-							const int j = __ffs(m) - 1;
+							const int j = __ffsll(static_cast<long long>(m)) - 1;
 							m &= m - 1;
-							L[o++] = static_cast<std::uint16_t>(j | (h << 5) | (lane << 6) | (((so[h] >> j) & 1u) << 11)
-																| (((scl[h] >> j) & 1u) << 12));
+							L[o++] = static_cast<std::uint16_t>(lb | static_cast<std::uint32_t>(j));
 						}
 					}
 					__syncwarp();
@@ -1109,13 +1110,18 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 						const std::uint32_t i	  = r0 + static_cast<std::uint32_t>(lane);
 						const bool			valid = i < total;
 						const std::uint32_t code  = valid ? L[i] : 0u;
-						const bool			isop  = BR && valid && ((code >> 11) & 1u);
-						const bool			iscl  = BR && valid && ((code >> 12) & 1u);
+						const std::uint32_t src	  = (code >> 6) & 31u, j6 = code & 63u;
+						bool				isop = false, iscl = false;
+						if constexpr (BR) {
+							const std::uint32_t o0 = __shfl_sync(kFull, so[0], src), o1 = __shfl_sync(kFull, so[1], src);
+							const std::uint32_t c0 = __shfl_sync(kFull, scl[0], src), c1 = __shfl_sync(kFull, scl[1], src);
+							isop = valid && ((((j6 >> 5) ? o1 : o0) >> (j6 & 31u)) & 1u);
+							iscl = valid && ((((j6 >> 5) ? c1 : c0) >> (j6 & 31u)) & 1u);
+						}
 						const std::uint32_t bo = BR ? __ballot_sync(kFull, isop) : 0u;
 						const std::uint32_t bc = BR ? __ballot_sync(kFull, iscl) : 0u;
 						if (valid) {
-							const unsigned long long q =
-								wq0 + 64u * ((code >> 6) & 31u) + 32u * ((code >> 5) & 1u) + (code & 31u);
+							const unsigned long long q = wq0 + 64u * src + j6;
 							const std::uint32_t pos = pbase + static_cast<std::uint32_t>(q - it.lo);
 							const std::uint32_t si	= si0 + i;
 							if (BATCH && si >= cap_s)
