@@ -748,13 +748,43 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 			}
 		};
 
+		// batch: does none of this warp's 2 KiB of the tile belong to the item's
+		// document?  (A small document leaves most warps of its tile idle.)
+		auto warp_outside = [&](const WsItem& it) -> bool {
+			const unsigned long long wlo = it.start + 2048ull * static_cast<unsigned>(warp);
+			return wlo + 2048 <= it.lo || wlo >= it.hi;
+		};
+
 		auto phase_a = [&](std::uint32_t k, WsFront& F) -> bool {
 			const WsItem		it	= item_of(k);
 			const int			s	= static_cast<int>(k & 1);
 			const int			buf = static_cast<int>(k % kBufs);
+			// every warp observes every phase of the slot's barrier, idle or not: a
+			// parity wait cannot tell a skipped phase from the one after it
 			if (!mbar_wait(&full_bar[s], (k >> 1) & 1u, res)) {
 				sc.failed = 1;
 				return false;
+			}
+			if (BATCH && warp_outside(it)) {
+				// no byte of the document: the identity element, nothing to classify
+				F		= WsFront {};
+				F.ex[3] = PATH == kPathEscape ? kIdent : 0u;
+				if (lane == 31)
+#pragma unroll
+					for (int i = 0; i < NE; ++i) sc.wtot[buf][warp][i] = (PATH == kPathEscape && i == 3) ? kIdent : 0u;
+				__syncwarp();
+				if (lane == 0)
+					mbar_arrive(&tot_bar[buf]);
+				if (warp == 0) {
+					if (!mbar_wait(&tot_bar[buf], (k / kBufs) & 1u, res)) {
+						sc.failed = 1;
+						return false;
+					}
+					if (lane == 0)
+						issue(k + 2);
+					__syncwarp();
+				}
+				return true;
 			}
 			unsigned char*			 stage = ring + s * kWsTile;
 			const unsigned long long q0	   = it.start + 64u * wtid;
@@ -928,6 +958,8 @@ __global__ void __launch_bounds__(WsGeom<W>::kThreads, 1)
 				sc.failed = 1;
 				return false;
 			}
+			if (BATCH && warp_outside(it))
+				return true;  // no byte of the document: nothing to write
 			const unsigned long long q0	 = it.start + 64u * wtid;
 			const std::uint32_t		 s_t = sc.state[buf];
 			const std::uint32_t		 p_t = (s_t >> 1) & 1u;
