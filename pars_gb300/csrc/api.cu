@@ -2,13 +2,13 @@
 //
 // One pars_ctx per device/thread.  It owns grow-only device buffers (scratch and
 // outputs), a pinned result block, and the loaded plans.  A scan is:
-//   k_scan<path>            fused R1..R5 (scan.cu)
-//   k_sort_pass(first=1)    speculative single counting-sort pass of R6 (pair.cu)
-//   k_pair(require_ok=1)    adjacent pairing + flags
+//   k_scan_ws<...> or k_scan<...>   fused R1..R5 (scan_ws*.cu, scan.cu)
+//   k_r6_count, k_r6_offsets, k_r6_scatter, k_pair_ranked
+//                                   R6 for keys within one 256-wide digit (pair.cu)
 //   D2H of the result block, one stream synchronisation
 // then host checks that may re-issue work: capacity overflow (grow, rerun), the
-// escape path's speculation guard (rerun on the generic kernel), and a key range
-// the single sort pass cannot take (LSD passes, then k_pair).
+// escape path's speculation guard (rerun on the general kernel), and a key range
+// the common case cannot take (LSD passes, then k_pair).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -49,27 +49,9 @@ const void* scan_ws_kernel(int path, bool brackets, int shape);
 int		   sort_tile_keys();
 const void* r6_kernel(int which);
 const void* bchar_gather_kernel();
-struct SortPass;
-__global__ void k_sort_pass(const SortPass p);
 __global__ void k_digit_hist(const std::int32_t* keys, const DevResult* res, unsigned int shift,
 							 unsigned int* hist);
 __global__ void k_pair(const PairArgs a, int require_sort_ok);
-
-struct SortPass {
-	const std::int32_t*	 keys_in;
-	const std::uint32_t* idx_in;
-	std::int32_t*		 keys_out;
-	std::uint32_t*		 idx_out;
-	const std::uint32_t* digit_hist;
-	std::uint64_t*		 lb;
-	Counters*			 ctr;
-	DevResult*			 res;
-	const unsigned int*	 key_hist;
-	unsigned long long	 cap;
-	unsigned int		 shift;
-	unsigned int		 epoch;
-	int					 first;
-};
 
 }  // namespace pars
 
@@ -637,6 +619,29 @@ int launch_pairs_speculative(pars_ctx* ctx, const Plan* pl, uint32_t flags, cuda
 	return 0;
 }
 
+// One stable LSD pass (k_lsd_count, k_lsd_offsets, k_lsd_scatter) over 8-bit digit
+// shift / 8 of the keys; the digit histogram must be in ctx->digit_hist.
+int lsd_pass(pars_ctx* ctx, const int32_t* kin, const uint32_t* iin, int32_t* kout, uint32_t* iout,
+			 const DevResult* res, unsigned shift, uint64_t n_cap, cudaStream_t st, uint64_t& launches) {
+	LsdPass lp {};
+	lp.keys_in	  = kin;
+	lp.idx_in	  = iin;
+	lp.keys_out	  = kout;
+	lp.idx_out	  = iout;
+	lp.tile_cnt	  = static_cast<uint32_t*>(ctx->lb.p);
+	lp.digit_hist = static_cast<const uint32_t*>(ctx->digit_hist.p);
+	lp.res		  = res;
+	lp.cap		  = n_cap;
+	lp.tiles_cap  = ctx->lb.cap / (256 * sizeof(uint32_t));
+	lp.shift	  = shift;
+	void* a[]	  = {&lp};
+	CK(cudaLaunchKernel(r6_kernel(4), dim3(ctx->num_sms * 4), dim3(256), a, 0, st));
+	CK(cudaLaunchKernel(r6_kernel(5), dim3(256), dim3(1024), a, 0, st));
+	CK(cudaLaunchKernel(r6_kernel(6), dim3(ctx->num_sms * 4), dim3(256), a, 0, st));
+	launches += 3;
+	return 0;
+}
+
 // Host-driven LSD sort when the speculative single pass could not run.
 int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t st,
 				   const DevResult& r) {
@@ -667,24 +672,9 @@ int pairs_fallback(pars_ctx* ctx, const Plan* pl, uint32_t flags, cudaStream_t s
 													   static_cast<unsigned int*>(ctx->digit_hist.p));
 		CK(cudaGetLastError());
 		ctx->launches++;
-		SortPass sp {};
-		sp.keys_in	  = kin;
-		sp.idx_in	  = iin;
-		sp.keys_out	  = (ps + 1 < passes) ? kbuf[out] : nullptr;
-		sp.idx_out	  = ibuf[out];
-		sp.digit_hist = static_cast<const uint32_t*>(ctx->digit_hist.p);
-		sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
-		sp.ctr		  = ctx->ctr;
-		sp.res		  = ctx->res;
-		sp.key_hist	  = ctx->key_hist;
-		sp.cap		  = n;
-		sp.shift	  = 8u * ps;
-		sp.epoch	  = next_epoch(ctx);
-		sp.first	  = 0;
-		void* a1[]	  = {&sp};
-		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4),
-							dim3(256), a1, 0, st));
-		ctx->launches++;
+		if (int e = lsd_pass(ctx, kin, iin, (ps + 1 < passes) ? kbuf[out] : nullptr, ibuf[out], ctx->res, 8u * ps,
+							 n, st, ctx->launches))
+			return e;
 		kin = kbuf[out];
 		iin = ibuf[out];
 		out ^= 1;
@@ -1532,11 +1522,10 @@ int lsd_sort_prepare(pars_ctx* ctx, uint64_t n_cap) {
 	return grow(ctx, ctx->sort_keys_a, n_cap * 4 + 16);
 }
 
-// clear_lb: clear the look-back words before every pass (a replayed graph repeats
-// its passes' epochs, so words of the previous replay must not be read as current).
+// The passes rewrite their per-tile counts completely, so a replayed graph reads
+// nothing of the previous replay.
 int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint32_t* order, uint64_t n_cap,
-			 DevResult* res, int passes, cudaStream_t st, bool clear_lb, uint64_t& launches) {
-	const uint64_t ntiles_sort = (n_cap + sort_tile_keys() - 1) / sort_tile_keys() + 1;
+			 DevResult* res, int passes, cudaStream_t st, uint64_t& launches) {
 	if (int e = lsd_sort_prepare(ctx, n_cap))
 		return e;
 	const int32_t*	kin	 = keys;
@@ -1546,28 +1535,12 @@ int lsd_sort(pars_ctx* ctx, const int32_t* keys, int32_t* kb, uint32_t* ib, uint
 	int				out		= (passes % 2 == 1) ? 0 : 1;
 	for (int ps = 0; ps < passes; ++ps) {
 		CK(cudaMemsetAsync(ctx->digit_hist.p, 0, 256 * 4, st));
-		if (clear_lb)
-			CK(cudaMemsetAsync(ctx->lb.p, 0, ntiles_sort * 256 * sizeof(uint64_t), st));
 		k_digit_hist<<<ctx->num_sms * 4, 256, 0, st>>>(kin, res, 8u * ps, static_cast<unsigned int*>(ctx->digit_hist.p));
 		CK(cudaGetLastError());
 		launches++;
-		SortPass sp {};
-		sp.keys_in	  = kin;
-		sp.idx_in	  = iin;
-		sp.keys_out	  = (ps + 1 < passes) ? kbuf[out] : nullptr;
-		sp.idx_out	  = ibuf[out];
-		sp.digit_hist = static_cast<const uint32_t*>(ctx->digit_hist.p);
-		sp.lb		  = static_cast<uint64_t*>(ctx->lb.p);
-		sp.ctr		  = ctx->ctr;
-		sp.res		  = res;
-		sp.key_hist	  = ctx->key_hist;
-		sp.cap		  = n_cap;
-		sp.shift	  = 8u * ps;
-		sp.epoch	  = next_epoch(ctx);
-		sp.first	  = 0;
-		void* a1[]	  = {&sp};
-		CK(cudaLaunchKernel(reinterpret_cast<const void*>(&k_sort_pass), dim3(ctx->num_sms * 4), dim3(256), a1, 0, st));
-		launches++;
+		if (int e = lsd_pass(ctx, kin, iin, (ps + 1 < passes) ? kbuf[out] : nullptr, ibuf[out], res, 8u * ps, n_cap, st,
+							 launches))
+			return e;
 		kin = kbuf[out];
 		iin = ibuf[out];
 		out ^= 1;
@@ -1797,7 +1770,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		uint64_t nl		 = 0;  // kernels of the sequence
 		// The batch's device work: every size and pointer in it follows from the
 		// layout key below, every count it reads lives in device memory.
-		auto launch_all = [&](bool clear_lb) -> int {
+		auto launch_all = [&]() -> int {
 		for (DevBuf* b : {&B.nstruct, &B.nopen, &B.nclose, &B.nbr, &B.unclosed, &B.flags, &B.cbase, &B.sbase,
 						  &B.bbase, &B.balanced, &B.well_formed, &B.max_depth})
 			CK(cudaMemsetAsync(b->p, 0, nd * 4, st));
@@ -1851,7 +1824,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 			if (run_pairs) {
 				if (int e = lsd_sort(ctx, static_cast<const int32_t*>(B.dkey.p), static_cast<int32_t*>(B.dkey_b.p),
 									 static_cast<uint32_t*>(B.order_b.p), static_cast<uint32_t*>(B.order.p), cap_b,
-									 B.bres, 4, st, clear_lb, nl))
+									 B.bres, 4, st, nl))
 					return e;
 				CK(cudaLaunchKernel(batch_kernel(2), dim3(grid), dim3(256), ra, 0, st));	 // segments
 				CK(cudaLaunchKernel(batch_kernel(3), dim3(grid), dim3(256), ra, 0, st));	 // pairs
@@ -1902,7 +1875,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 				}
 			if (!done && repeat) {
 				CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-				const int	rc = launch_all(true);
+				const int	rc = launch_all();
 				cudaGraph_t graph = nullptr;
 				const cudaError_t ec = cudaStreamEndCapture(st, &graph);
 				if (rc) {
@@ -1934,7 +1907,7 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		}
 		if (!done) {
 			nl = 0;
-			if (int rc = launch_all(false))
+			if (int rc = launch_all())
 				return rc;
 			ctx->launches += nl;
 		}

@@ -8,24 +8,19 @@
 // well_formed = every pair typed + even count + balanced; max_depth = max(0, bal).
 //
 // The scan kernel already produced the keys (depth[]), their extrema and a
-// 2048-bin histogram over [-1024, 1024), so R6 here is:
-//   k_sort_pass  one stable counting-sort pass (onesweep: per-tile ranks with
-//                warp match-any, per-bucket decoupled look-back across tiles) on an
-//                8-bit digit of key - min_key, writing (optionally) keys and the
-//                bracket index;
-//   k_digit_hist the digit histogram for passes the scan's window cannot provide;
-//   k_pair       adjacent pairing + type check, then the last CTA folds the flags.
-// The common case (key range <= 256, all keys in the window) runs without a host
-// round-trip and without look-back chains:
+// 2048-bin histogram over [-1024, 1024).  The common case (key range <= 256, all
+// keys in the window) runs without a host round-trip and without look-back chains:
 //   k_r6_count    per-tile digit counts (tiles of 4096 keys, warp match-any);
 //   k_r6_offsets  per digit, the exclusive scan of its counts over tiles plus the
 //                 digit's global base (from the scan's key histogram);
 //   k_r6_scatter  stable ranks again, each bracket to its sorted slot, with its
 //                 structural index and byte beside it, and its slot recorded;
 //   k_pair_ranked each bracket reads its partner's slot and writes its own
-//                 entries in order (no scattered writes).
-// Anything else is finished by the host with k_sort_pass LSD passes over 8-bit
-// digits.
+//                 entries in order (no scattered writes), then the last CTA folds
+//                 the flags.
+// Anything else is finished by the host with LSD passes over 8-bit digits, each the
+// same three steps (k_digit_hist for the digit's histogram, then k_lsd_count,
+// k_lsd_offsets, k_lsd_scatter), and k_pair over the sorted order.
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -40,187 +35,6 @@ constexpr int	   kSortItems	  = 16;
 constexpr int	   kSortTile	  = kSortThreads * kSortItems;	// 4096 keys
 constexpr int	   kSortWarps	  = kSortThreads / 32;
 
-// Look-back word of one (tile, bucket): flag(2) | epoch(22) | count(40).
-__device__ __forceinline__ std::uint64_t pack_lb(std::uint32_t flag, std::uint32_t epoch,
-												 std::uint64_t cnt) {
-	return (static_cast<std::uint64_t>(flag) << 62)
-		 | (static_cast<std::uint64_t>(epoch & 0x3FFFFFu) << 40) | (cnt & 0xFFFFFFFFFFull);
-}
-
-}  // namespace
-
-struct SortPass {
-	const std::int32_t*	 keys_in;	 // [n]
-	const std::uint32_t* idx_in;	 // [n] or null (identity)
-	std::int32_t*		 keys_out;	 // [n] or null
-	std::uint32_t*		 idx_out;	 // [n]
-	const std::uint32_t* digit_hist; // [256] or null: take it from the key window
-	std::uint64_t*		 lb;		 // look-back words [tiles][256]
-	Counters*			 ctr;
-	DevResult*			 res;
-	const unsigned int*	 key_hist;	 // [2048] window histogram
-	unsigned long long	 cap;		 // capacity of the key / index buffers
-	unsigned int		 shift;
-	unsigned int		 epoch;
-	int					 first;		 // 1: the speculative single pass (checks the range)
-};
-
-// One stable counting-sort pass over digit = ((key - min_key) >> shift) & 255.
-__global__ void __launch_bounds__(kSortThreads) k_sort_pass(const SortPass p) {
-	__shared__ unsigned int whist[kSortWarps][256];
-	__shared__ unsigned int gbase[256];
-	__shared__ unsigned int texcl[256];
-	__shared__ unsigned long long s_tile;
-	__shared__ int			s_fail;
-
-	DevResult* res = p.res;
-	const int  tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const unsigned long long n = res->n_brackets;
-	const long long			 kmin = n ? dec_min(res->min_key) : 0;
-
-	if (p.first) {
-		// speculative single pass: only when every key sits in the window and the
-		// key range fits one 8-bit digit
-		const bool ok = !res->keys_oob && !res->error && n <= p.cap
-					 && (n == 0 || dec_max(res->max_key) - kmin < 256);
-		if (blockIdx.x == 0 && tid == 0)
-			res->sort_ok = ok ? 1u : 0u;
-		if (!ok || n == 0)
-			return;
-	}
-	// global base of each digit bucket
-	{
-		unsigned int c = 0;
-		if (p.digit_hist) {
-			c = p.digit_hist[tid];
-		} else {
-			const long long k = kmin + tid;
-			if (k >= -kKeyWindow && k < kKeyWindow)
-				c = p.key_hist[k + kKeyWindow];
-		}
-		// block exclusive scan of 256 counts
-		unsigned int x = c;
-#pragma unroll
-		for (int off = 1; off < 32; off <<= 1) {
-			const unsigned int y = __shfl_up_sync(kFull, x, off);
-			if (lane >= off)
-				x += y;
-		}
-		if (lane == 31)
-			whist[0][warp] = x;
-		__syncthreads();
-		unsigned int wpre = 0;
-		for (int w = 0; w < warp; ++w) wpre += whist[0][w];
-		gbase[tid] = wpre + x - c;
-		__syncthreads();
-	}
-	const std::uint32_t epoch = p.epoch & 0x3FFFFFu;
-	const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
-	if (tid == 0)
-		s_fail = 0;
-	while (true) {
-		if (tid == 0)
-			s_tile = atomicAdd(&p.ctr->sort_ticket, 1u);
-		for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
-		__syncthreads();
-		const unsigned long long t = s_tile;
-		if (t >= ntiles || s_fail)
-			break;
-		// ---- rank: warp w owns 512 consecutive keys, 16 rounds of 32 ----------------
-		const unsigned long long wbase = t * kSortTile + static_cast<unsigned long long>(warp) * 512;
-		std::uint32_t			 dig[kSortItems];
-		std::uint32_t			 rnk[kSortItems];
-#pragma unroll
-		for (int i = 0; i < kSortItems; ++i) {
-			const unsigned long long e = wbase + i * 32 + lane;
-			std::uint32_t			 d = 0xFFFFFFFFu;
-			if (e < n)
-				d = static_cast<std::uint32_t>(
-						static_cast<unsigned long long>(p.keys_in[e] - kmin) >> p.shift)
-				  & 255u;
-			const std::uint32_t peers = __match_any_sync(kFull, d);
-			const std::uint32_t below = peers & ((1u << lane) - 1u);
-			std::uint32_t		base  = 0;
-			if (d != 0xFFFFFFFFu)
-				base = whist[warp][d];
-			__syncwarp();
-			if (d != 0xFFFFFFFFu && below == 0)
-				whist[warp][d] = base + __popc(peers);
-			__syncwarp();
-			dig[i] = d;
-			rnk[i] = base + __popc(below);
-		}
-		__syncthreads();
-		// ---- per-bucket tile total and warp offsets ----------------------------------
-		unsigned int tot = 0;
-		for (int w = 0; w < kSortWarps; ++w) {
-			const unsigned int c = whist[w][tid];
-			whist[w][tid]		 = tot;	 // becomes the warp's exclusive offset
-			tot += c;
-		}
-		// ---- per-bucket decoupled look-back ------------------------------------------
-		std::uint64_t* row = p.lb + t * 256;
-		unsigned long long excl = 0;
-		if (t == 0) {
-			st_release64(&row[tid], pack_lb(kFlagIncl, epoch, tot));
-		} else {
-			st_release64(&row[tid], pack_lb(kFlagAgg, epoch, tot));
-			long long j	   = static_cast<long long>(t) - 1;
-			std::uint32_t spins = 0;
-			while (j >= 0) {
-				const std::uint64_t w = ld_acquire64(p.lb + j * 256 + tid);
-				const std::uint32_t f = static_cast<std::uint32_t>(w >> 62);
-				const std::uint32_t e = static_cast<std::uint32_t>(w >> 40) & 0x3FFFFFu;
-				if (e != epoch || f == 0) {
-					if (++spins > kSpinLimit) {
-						record_error(res, kDevErrTimeout);
-						s_fail = 1;
-						break;
-					}
-					if ((spins & 63u) == 0 && aborted(res)) {
-						s_fail = 1;
-						break;
-					}
-					__nanosleep(64);
-					continue;
-				}
-				excl += w & 0xFFFFFFFFFFull;
-				if (f == kFlagIncl)
-					break;
-				--j;
-			}
-			st_release64(&row[tid], pack_lb(kFlagIncl, epoch, excl + tot));
-		}
-		texcl[tid] = static_cast<unsigned int>(excl);
-		__syncthreads();
-		// ---- scatter ----------------------------------------------------------------
-#pragma unroll
-		for (int i = 0; i < kSortItems; ++i) {
-			const unsigned long long e = wbase + i * 32 + lane;
-			const std::uint32_t		 d = dig[i];
-			if (d == 0xFFFFFFFFu)
-				continue;
-			const unsigned long long dst =
-				static_cast<unsigned long long>(gbase[d]) + texcl[d] + whist[warp][d] + rnk[i];
-			p.idx_out[dst] = p.idx_in ? p.idx_in[e] : static_cast<std::uint32_t>(e);
-			if (p.keys_out)
-				p.keys_out[dst] = p.keys_in[e];
-		}
-		__syncthreads();
-	}
-	__syncthreads();
-	if (tid == 0) {
-		__threadfence();
-		const unsigned int done = atomicAdd(&p.ctr->sort_done, 1u);
-		if (done == gridDim.x - 1) {
-			p.ctr->sort_ticket = 0;
-			p.ctr->sort_done   = 0;
-			__threadfence();
-		}
-	}
-}
-
-namespace {
 
 // The common case holds: every key in the window, the range within one digit, the
 // outputs within capacity.  Writes sort_ok (block 0, thread 0).
@@ -399,6 +213,158 @@ __global__ void __launch_bounds__(kSortThreads) k_r6_scatter(const R6Sort p) {
 			p.order[dst]	 = static_cast<std::uint32_t>(e);
 			p.sorted_si[dst] = sis[i];
 			p.sorted_ch[dst] = chs[i];
+		}
+		__syncthreads();
+	}
+}
+
+// ---- LSD passes (keys outside the window or wider than one digit, and the batch's
+// (document, depth) keys): the common case's three steps on one digit each -------
+namespace {
+
+__device__ __forceinline__ bool lsd_common(const LsdPass& p, unsigned long long& n, long long& kmin,
+										   unsigned long long& tiles) {
+	n	  = p.res->n_brackets;
+	kmin  = n ? dec_min(p.res->min_key) : 0;  // as k_digit_hist
+	tiles = (n + kSortTile - 1) / kSortTile;
+	return n && n <= p.cap && tiles <= p.tiles_cap && !p.res->error;
+}
+
+__device__ __forceinline__ std::uint32_t lsd_digit(const LsdPass& p, std::int32_t key, long long kmin) {
+	return static_cast<std::uint32_t>(static_cast<unsigned long long>(key - kmin) >> p.shift) & 255u;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kSortThreads) k_lsd_count(const LsdPass p) {
+	__shared__ unsigned int hist[256];
+	unsigned long long		n, tiles;
+	long long				kmin;
+	if (!lsd_common(p, n, kmin, tiles))
+		return;
+	const int tid = threadIdx.x;
+	for (unsigned long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+		std::uint32_t dg[kSortItems];
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = t * kSortTile + static_cast<unsigned long long>(i) * kSortThreads + tid;
+			dg[i] = e < n ? lsd_digit(p, p.keys_in[e], kmin) : 0xFFFFFFFFu;
+		}
+		hist[tid] = 0;
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const std::uint32_t peers = __match_any_sync(kFull, dg[i]);
+			if (dg[i] != 0xFFFFFFFFu && (peers & ((1u << (tid & 31)) - 1u)) == 0)
+				atomicAdd(&hist[dg[i]], static_cast<unsigned int>(__popc(peers)));
+		}
+		__syncthreads();
+		p.tile_cnt[static_cast<unsigned long long>(tid) * tiles + t] = hist[tid];
+		__syncthreads();
+	}
+}
+
+// One block per digit: the digit's base (histogram of the smaller digits) + the
+// exclusive scan of its tile counts.
+__global__ void __launch_bounds__(1024) k_lsd_offsets(const LsdPass p) {
+	__shared__ unsigned int wsum[32];
+	__shared__ unsigned int s_carry;
+	unsigned long long		n, tiles;
+	long long				kmin;
+	if (!lsd_common(p, n, kmin, tiles))
+		return;
+	const int		   tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const unsigned int d   = blockIdx.x;
+	unsigned int	   c   = static_cast<unsigned int>(tid) < d ? p.digit_hist[tid] : 0u;
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+	if (lane == 0)
+		wsum[warp] = c;
+	__syncthreads();
+	if (tid == 0) {
+		unsigned int b = 0;
+		for (int w = 0; w < 32; ++w) b += wsum[w];
+		s_carry = b;
+	}
+	__syncthreads();
+	std::uint32_t* row = p.tile_cnt + static_cast<unsigned long long>(d) * tiles;
+	for (unsigned long long t0 = 0; t0 < tiles; t0 += 1024) {
+		const unsigned long long t = t0 + tid;
+		const unsigned int		 v = t < tiles ? row[t] : 0u;
+		unsigned int			 x = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const unsigned int y = __shfl_up_sync(kFull, x, o);
+			if (lane >= o)
+				x += y;
+		}
+		if (lane == 31)
+			wsum[warp] = x;
+		__syncthreads();
+		unsigned int wp = 0;
+		for (int w = 0; w < warp; ++w) wp += wsum[w];
+		const unsigned int carry = s_carry;
+		if (t < tiles)
+			row[t] = carry + wp + x - v;
+		__syncthreads();
+		if (tid == 1023)
+			s_carry = carry + wp + x;
+		__syncthreads();
+	}
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_lsd_scatter(const LsdPass p) {
+	__shared__ unsigned int whist[kSortWarps][256];
+	unsigned long long		n, tiles;
+	long long				kmin;
+	if (!lsd_common(p, n, kmin, tiles))
+		return;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	for (unsigned long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+		const unsigned long long wbase = t * kSortTile + static_cast<unsigned long long>(warp) * 512;
+		std::uint32_t			 dig[kSortItems], rnk[kSortItems], idx[kSortItems];
+		std::int32_t			 key[kSortItems];
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const unsigned long long e = wbase + i * 32 + lane;
+			key[i]					   = e < n ? p.keys_in[e] : 0;
+			idx[i]					   = e < n ? (p.idx_in ? p.idx_in[e] : static_cast<std::uint32_t>(e)) : 0u;
+			dig[i]					   = e < n ? lsd_digit(p, key[i], kmin) : 0xFFFFFFFFu;
+		}
+		for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			const std::uint32_t d	  = dig[i];
+			const std::uint32_t peers = __match_any_sync(kFull, d);
+			const std::uint32_t below = peers & ((1u << lane) - 1u);
+			std::uint32_t		base  = 0;
+			if (d != 0xFFFFFFFFu)
+				base = whist[warp][d];
+			__syncwarp();
+			if (d != 0xFFFFFFFFu && below == 0)
+				whist[warp][d] = base + __popc(peers);
+			__syncwarp();
+			rnk[i] = base + __popc(below);
+		}
+		__syncthreads();
+		{
+			unsigned int off = p.tile_cnt[static_cast<unsigned long long>(tid) * tiles + t];
+			for (int w = 0; w < kSortWarps; ++w) {
+				const unsigned int c = whist[w][tid];
+				whist[w][tid]		 = off;
+				off += c;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kSortItems; ++i) {
+			if (dig[i] == 0xFFFFFFFFu)
+				continue;
+			const std::uint32_t dst = whist[warp][dig[i]] + rnk[i];
+			if (dst >= n)
+				continue;  // unreachable while the digit histogram matches the keys
+			p.idx_out[dst] = idx[i];
+			if (p.keys_out)
+				p.keys_out[dst] = key[i];
 		}
 		__syncthreads();
 	}
@@ -593,6 +559,9 @@ const void* r6_kernel(int which) {
 		case 1: return reinterpret_cast<const void*>(&k_r6_offsets);
 		case 2: return reinterpret_cast<const void*>(&k_r6_scatter);
 		case 3: return reinterpret_cast<const void*>(&k_pair_ranked);
+		case 4: return reinterpret_cast<const void*>(&k_lsd_count);
+		case 5: return reinterpret_cast<const void*>(&k_lsd_offsets);
+		case 6: return reinterpret_cast<const void*>(&k_lsd_scatter);
 		default: return nullptr;
 	}
 }

@@ -252,6 +252,22 @@ struct R6Sort {
 	unsigned long long	 tiles_cap; // tiles the tile_cnt buffer holds
 };
 
+// One stable LSD pass over digit ((key - min_key) >> shift) & 255 of n = res->n_brackets
+// keys: per-tile digit counts, a per-digit scan over tiles seeded by the digit
+// histogram, a stable scatter of (key, index).
+struct LsdPass {
+	const std::int32_t*	 keys_in;
+	const std::uint32_t* idx_in;	 // null: the identity
+	std::int32_t*		 keys_out;	 // null: not needed (last pass)
+	std::uint32_t*		 idx_out;
+	std::uint32_t*		 tile_cnt;	 // [256][tiles]
+	const std::uint32_t* digit_hist; // [256] this digit's histogram
+	const DevResult*	 res;
+	unsigned long long	 cap;
+	unsigned long long	 tiles_cap;
+	unsigned int		 shift;
+};
+
 struct PairArgs {
 	const std::int32_t*	 depth;		// [n_brackets] keys
 	const std::uint8_t*	 bchar;		// bracket bytes written by the scan (when `in` is null)
