@@ -7,7 +7,8 @@
 //   k_batch_compact   regions -> one dense bracket array; composite key
 //                     document << 11 | (depth key + 1024)
 //   k_batch_docs      each document's dense bracket base
-//   4 x (k_digit_hist, k_sort_pass)   stable LSD sort of the composite keys
+//   4 x (k_digit_hist, k_lsd_count, k_lsd_offsets, k_lsd_scatter)
+//                     stable LSD sort of the composite keys
 //   k_batch_segstart  each document's segment start in (document, key) order
 //   k_batch_pair      adjacent pairing within each document's segment + type check
 //   k_batch_finalize  balanced / well_formed / max_depth per document

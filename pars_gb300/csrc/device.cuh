@@ -6,7 +6,7 @@
 //                the warp-specialised kernel keeps 64-bit self-validating
 //                aggregate words per tile instead
 //   DevResult    one per scan: counts, depth extrema, flags
-//   Counters     dynamic tile tickets and CTA-exit counters (self-resetting)
+//   Counters     CTA-exit counter of the pairing kernels (self-resetting)
 //   key_hist     2048-bin histogram of bracket depth keys in [-1024, 1024)
 #pragma once
 
@@ -39,10 +39,8 @@ struct __align__(64) TileDescG {   // generic path: one nibble-packed map per de
 };
 
 struct Counters {
-	unsigned int scan_ticket, scan_done;
-	unsigned int sort_ticket, sort_done;
-	unsigned int pair_done;
-	unsigned int pad[11];
+	unsigned int pair_done;	 // CTAs of k_pair / k_pair_ranked done (the last folds the flags)
+	unsigned int pad[15];
 };
 
 // ---- PTX helpers --------------------------------------------------------------
