@@ -332,3 +332,14 @@ def test_chunked_equals_whole(ctx, grammar):
 def test_empty(scanners):
     r = scanners["json"].scan_device(0, 0, want_pairs=True)
     assert r.n_struct == 0 and r.balanced and r.well_formed and r.max_depth == 0
+
+
+@pytest.mark.parametrize("depth", [300, 70_000])
+@pytest.mark.parametrize("tail", [b"", b"]]]", b"[[["])
+def test_nesting_beyond_one_digit(scanners, depth, tail):
+    """Depth keys spanning more than one 8-bit digit (two and three LSD passes),
+    balanced and unbalanced: every output against the oracle."""
+    plan = plan_bytes("json")
+    data = np.frombuffer(b"[" * depth + b"1" + b"]" * depth + tail, np.uint8).copy()
+    e = expected_from_oracle(plan, data)
+    compare(run(scanners["json"], data), e, f"depth {depth} + {tail!r}")
