@@ -44,11 +44,13 @@ SEED = 20261203
 
 
 def peaks():
-    for p in (os.path.join(ROOT, "MEASURED_PEAKS.json"), "/root/repo/MEASURED_PEAKS.json"):
-        if os.path.exists(p):
-            with open(p) as f:
-                d = json.load(f)
-            return float(d["hbm_gbs"]), "measured"
+    """HBM copy bandwidth measured on this GPU type (MEASURED_PEAKS.json at the
+    repository root), else the 6.8 TB/s fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
 
 
