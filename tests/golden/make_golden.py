@@ -4,6 +4,7 @@ backend (built by ``make -C oracle ref`` from the reference headers where they l
 Run where the reference sources exist:
 
     make -C oracle ref && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py published <reference>/paper/plots/data/pars.csv
 
 Writes tests/golden/<grammar>.npz: for every case, the input bytes and the reference
 outputs (positions, chars, bracket_pos, bracket_char, pair [bracket-index space],
@@ -34,6 +35,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from pars_gb300 import synth  # noqa: E402
 
+sys.path.insert(0, HERE)
+from bench_records import PUBLISHED, RECORDS  # noqa: E402
+
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
 ALPHABETS = {
@@ -43,16 +47,6 @@ ALPHABETS = {
     "clike": b"{};/*\n abc123",
     "ini": b"[]=;\n abc0123",
     "xml": b"<>/=?!\"' ab0123",
-}
-
-RECORDS = {
-    "json": b"{\"id\":123,\"name\":\"x \\\"y\\\"\",\"a\":[1,2,3],\"n\":{\"z\":null}}",
-    "csv": b"alpha,beta,\"quoted, field\",\"has \"\"q\"\"\",42,true\n",
-    "toml": (b"[server]\nhost = \"localhost\"\nport = 8080\nname = 'a # b'\n"
-             b"# comment { } , = with \"quotes\"\narr = [1, 2, 3]\n"),
-    "clike": b"int x; /* c { ; } */ y = 1; // { ; }\n",
-    "ini": b"[section]\nkey = value\nnum = 123\n; comment\nother = x\n",
-    "xml": b"<item id=\"1\" name=\"x &amp; y\">alpha</item>",
 }
 
 
@@ -128,7 +122,36 @@ def run_ref(g: str, data: bytes, tmp: str) -> dict[str, np.ndarray]:
     return r
 
 
+def published(csv_path: str) -> None:
+    """Write published_tokens.json from the reference's table of benchmark runs
+    (paper/plots/data/pars.csv: format, impl, variant, scale_mb, five GB/s columns,
+    tokens, bytes_moved).  Every variant of a (format, scale) reports the same
+    token count; the N2 variant moves exactly the payload to the device, so its
+    bytes_moved is the payload size."""
+    import csv
+    import json
+    rows: dict[tuple[str, int], dict] = {}
+    with open(csv_path) as f:
+        for r in csv.reader(line for line in f if not line.startswith("#")):
+            if len(r) < 11 or r[1] != "pars":
+                continue
+            key = (r[0], int(r[3]))
+            e = rows.setdefault(key, {"grammar": r[0], "scale_mb": int(r[3]),
+                                      "tokens": int(r[9]), "bytes": None})
+            if e["tokens"] != int(r[9]):
+                sys.exit(f"token counts differ between variants of {key}")
+            if r[2] == "N2":
+                e["bytes"] = int(r[10])
+    out = sorted(rows.values(), key=lambda e: (e["grammar"], e["scale_mb"]))
+    with open(PUBLISHED, "w") as f:
+        f.write("[\n" + ",\n".join(json.dumps(e) for e in out) + "\n]\n")
+    print(len(out), "published (grammar, scale) entries")
+
+
 def main() -> None:
+    if len(sys.argv) == 3 and sys.argv[1] == "published":
+        published(sys.argv[2])
+        return
     if not os.path.exists(DRIVER):
         sys.exit("oracle/_ref/ref_driver missing: run `make -C oracle ref` first")
     with tempfile.TemporaryDirectory() as tmp:

@@ -7,14 +7,18 @@ sources) the oracle is additionally compared on fresh random inputs.
 """
 import os
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
 import pytest
 
-from conftest import GRAMMARS, ROOT, golden_cases, plan_bytes
+from conftest import GOLDEN, GRAMMARS, ROOT, golden_cases, plan_bytes
 from oracle import oracle
 from pars_gb300 import synth
+
+sys.path.insert(0, GOLDEN)
+import bench_records  # noqa: E402
 
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
@@ -70,6 +74,38 @@ def test_pair_struct_space_roundtrip():
     nb = np.ones(sr.positions.size, bool)
     nb[bsi] = False
     assert np.all(ps[nb] == -1)
+
+
+def test_benchmark_payload_sizes():
+    """The payload builder restates bench/bench_boundary.cu:315-336: its sizes are
+    the input sizes the reference reports for all 42 published runs."""
+    pub = bench_records.published()
+    assert len(pub) == 42 and {e["grammar"] for e in pub} == set(GRAMMARS)
+    for e in pub:
+        target = e["scale_mb"] << 20
+        assert bench_records.payload_size(e["grammar"], target) == e["bytes"], e
+    for g in GRAMMARS:
+        for target in (1, 100, 4096, 1 << 20):
+            assert bench_records.payload(g, target).size == bench_records.payload_size(g, target)
+
+
+@pytest.mark.parametrize("grammar", GRAMMARS)
+def test_oracle_published_token_counts(grammar):
+    """The oracle's structural count on the reference's benchmark payloads equals
+    the token count the reference published (paper/plots/data/pars.csv) at every
+    scale up to 64 MiB, and the offsets are one unit's offsets tiled, which is what
+    lets the GPU test check the 128-512 MiB runs without the oracle."""
+    plan = plan_bytes(grammar)
+    unit_pos = oracle.scan(plan, np.frombuffer(bench_records.unit(grammar), np.uint8)).positions
+    for e in bench_records.published():
+        if e["grammar"] != grammar or e["scale_mb"] > 64:
+            continue
+        target = e["scale_mb"] << 20
+        data = bench_records.payload(grammar, target)
+        sr = oracle.scan(plan, data)
+        assert sr.positions.size == e["tokens"], e
+        tiled = bench_records.tiled_positions(grammar, target, unit_pos)
+        assert np.array_equal(sr.positions.astype(np.int64), tiled), e
 
 
 @pytest.mark.skipif(not os.path.exists(DRIVER), reason="reference sources not built here")

@@ -3,16 +3,21 @@ reference CPU backend) and against the CPU oracle, bit-exact for every output:
 structural offsets, chars, bracket offsets/chars, depth keys, pairs (bracket and
 structural index space), per-byte masks, and the balanced / well_formed /
 max_depth / unclosed_mode flags."""
+import sys
+
 import numpy as np
 import pytest
 
-from conftest import GRAMMARS, golden_cases, plan_bytes
+from conftest import GOLDEN, GRAMMARS, golden_cases, plan_bytes
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 from oracle import oracle  # noqa: E402
 from pars_gb300 import Context, Scanner, synth  # noqa: E402
+
+sys.path.insert(0, GOLDEN)
+import bench_records  # noqa: E402
 
 
 @pytest.fixture(scope="module")
@@ -197,6 +202,50 @@ def test_csv_full_size_properties(scanners):
     assert np.all(np.isin(data[pos], np.frombuffer(b",\n", np.uint8)))
     e = expected_from_oracle(plan, data)
     compare(g, e, "csv1g")
+
+
+@pytest.mark.parametrize("grammar", GRAMMARS)
+def test_published_token_counts(scanners, grammar):
+    """The reference's benchmark payloads (bench/bench_boundary.cu:315-336) at every
+    scale the reference published, 8-512 MiB: the structural count equals its
+    published token count (paper/plots/data/pars.csv), the offsets and chars are one
+    unit's (from the oracle) tiled, and the flags are the oracle's on 8 MiB."""
+    plan = plan_bytes(grammar)
+    sc = scanners[grammar]
+    runs = [e for e in bench_records.published() if e["grammar"] == grammar]
+    assert len(runs) == 7
+    big = bench_records.payload(grammar, max(e["scale_mb"] for e in runs) << 20)
+    buf = torch.from_numpy(big).cuda()
+    ur = oracle.scan(plan, np.frombuffer(bench_records.unit(grammar), np.uint8))
+    unit_pos = torch.from_numpy(ur.positions.astype(np.int64)).cuda()
+    unit_chars = torch.from_numpy(ur.chars.copy()).cuda()
+    sr = oracle.scan(plan, bench_records.payload(grammar, 8 << 20))
+    pr = oracle.pair(plan, sr.bracket_char)
+    flags = (sr.unclosed_mode, pr.balanced, pr.well_formed, pr.max_depth)
+    u, js = len(bench_records.unit(grammar)), grammar == "json"
+    for e in runs:
+        n, k = e["bytes"], bench_records.units(grammar, e["scale_mb"] << 20)
+        if js:  # a shorter payload is a prefix of the longest, closed by ']'
+            sep = int(buf[n - 1].item())
+            buf[n - 1] = ord("]")
+        r = sc.scan_device(buf.data_ptr(), n, want_pairs=True, want_chars=True)
+        torch.cuda.synchronize()
+        assert r.n_struct == e["tokens"], e
+        base = torch.arange(k, device="cuda", dtype=torch.int64) * u + (1 if js else 0)
+        exp_pos = (base[:, None] + unit_pos[None, :]).flatten()
+        exp_chars = unit_chars.repeat(k)
+        if js:
+            exp_pos = torch.cat([torch.zeros(1, dtype=torch.int64, device="cuda"), exp_pos])
+            exp_chars = torch.cat([torch.tensor([ord("[")], dtype=torch.uint8, device="cuda"),
+                                   exp_chars])
+            exp_chars[-1] = ord("]")
+        got_pos = r.structural().view(torch.int32).to(torch.int64)
+        assert torch.equal(got_pos, exp_pos), e
+        assert torch.equal(r.chars(), exp_chars), e
+        assert (r.unclosed_mode, r.balanced, r.well_formed, r.max_depth) == flags, e
+        if js:
+            buf[n - 1] = sep
+        del got_pos, exp_pos, exp_chars, base
 
 
 def test_scan_host_matches_device(scanners):
