@@ -167,6 +167,34 @@ def cpu_baseline(plan_bytes: bytes, data: np.ndarray, budget_s: float = 10.0):
                       f"{t_total:.1f} s; the reference scan is sequential per document"}
 
 
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_batch_baseline(groups, what: str, budget_s: float = 2.0):
+    """The oracle port (scan + pair per document) over every document of `groups`
+    ([(plan bytes, concatenated bytes, offsets)]), each group's documents spread
+    over all host threads; GB/s of the documents' bytes."""
+    from oracle import oracle
+    threads = host_threads()
+    nbytes = sum(int(o[-1] - o[0]) for _, _, o in groups)
+
+    def one_pass():
+        return sum(oracle.time_batch(p, d, o, threads)[0] for p, d, o in groups)
+    one_pass()  # warm-up: page in the documents, grow the threads' scratch
+    t_total, passes = 0.0, 0
+    while t_total < budget_s and passes < 20:
+        t_total += one_pass()
+        passes += 1
+    return {"value": round(nbytes * passes / t_total / 1e9, 4), "unit": "GB/s",
+            "cores": threads, "kind": "port",
+            "sample": f"{what}: {passes} pass(es), {t_total:.2f} s; documents spread over "
+                      f"{threads} host threads (the reference scans each document sequentially)"}
+
+
 def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
     """The slowest rank's time (ms): replicas finish when the last one does."""
     if dist is None:
@@ -270,7 +298,7 @@ def general_leg(ctx, stream, barrier, peak, nbytes=64 << 20, steps=10):
             "documents": out}
 
 
-def batched_leg(args, stream, barrier, world, peak, ndocs=100_000, sample=2000):
+def batched_leg(args, stream, barrier, world, peak, ndocs=100_000, sample=2000, cpu=False):
     """Batched JSON (100,000 documents, log-normal sizes: median 2 KiB, sigma 1.5,
     clamped to 64 B - 4 MiB): one pars_scan_batch call per step (device-resident
     input, blocking, host planning included) against one pars_scan_device launch per
@@ -308,16 +336,19 @@ def batched_leg(args, stream, barrier, world, peak, ndocs=100_000, sample=2000):
     n = int(data.size)
     batch_gbps = world * n / batch_s / 1e9
     per_doc_gbps = sb / per_doc_s / 1e9
+    cpu_line = (cpu_batch_baseline([(plan("json"), data, offs)], f"all {ndocs} documents")
+                if cpu else None)
     return {"workload": "json_batch_100k_lognormal_docs", "docs": ndocs, "bytes": n,
             "GBps": round(batch_gbps, 3), "ms_per_batch": round(batch_s * 1e3, 3),
             "per_doc_launch_GBps": round(per_doc_gbps, 3),
             "per_doc_launch_sample": f"{len(pick)} seeded documents, {sb} bytes, one pars_scan_device each",
             "speedup_vs_per_doc_launch": round(batch_gbps / per_doc_gbps, 2),
             "recomputed_docs": int(r.n_recomputed), "grid": int(r.grid),
-            "timing": "wall clock of the blocking call, host planning and result flags included"}
+            "timing": "wall clock of the blocking call, host planning and result flags included",
+            "cpu_baseline": cpu_line}
 
 
-def serving_leg(args, seconds=0.6, loads=(0.1, 0.5, 0.9, 1.2)):
+def serving_leg(args, seconds=0.6, loads=(0.1, 0.5, 0.9, 1.2), cpu=False):
     """Serving: Poisson arrivals of mixed requests (70% JSON, 30% CSV, sizes
     log-uniform 256 B - 64 MiB, drawn from a seeded pool of pinned documents),
     memory-admitted into an 8 GiB device arena.  Capacity is the throughput with all
@@ -397,6 +428,14 @@ def serving_leg(args, seconds=0.6, loads=(0.1, 0.5, 0.9, 1.2)):
     for srv in paths.values():
         srv.close()
     out["timing"] = "latency = completion - submission (server steady clock), results in host memory"
+    if cpu:
+        groups = []
+        for g in ("json", "csv"):
+            docs = [t.numpy() for gg, t in pool if gg == g]
+            offs = np.concatenate([[0], np.cumsum([d.size for d in docs])]).astype(np.uint64)
+            groups.append((plan(g), np.concatenate(docs), offs))
+        out["cpu_baseline"] = cpu_batch_baseline(
+            groups, f"the {len(pool)}-document request pool, JSON documents then CSV documents")
     return out
 
 
@@ -529,15 +568,17 @@ def main():
     if not args.no_secondary:
         general = general_leg(sc.ctx, stream, barrier, peak)
 
+    # CPU baselines on rank 0 of a one-GPU run only
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu
     batched = None
     if not args.no_batched:
-        batched = batched_leg(args, stream, barrier, world, peak)
+        batched = batched_leg(args, stream, barrier, world, peak, cpu=want_cpu)
     serving = None
     if not args.no_serving and rank == 0:
-        serving = serving_leg(args)
+        serving = serving_leg(args, cpu=want_cpu)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if want_cpu:
         cpu = cpu_baseline(plan("csv"), data)
 
     if rank == 0:

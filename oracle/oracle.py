@@ -43,6 +43,8 @@ def lib():
         L.oracle_pair.argtypes = [vp, u64, vp, u64, vp, vp, vp]
         L.oracle_time_scan_pair.restype = ctypes.c_double
         L.oracle_time_scan_pair.argtypes = [vp, u64, vp, u64, i32, vp]
+        L.oracle_time_batch.restype = ctypes.c_double
+        L.oracle_time_batch.argtypes = [vp, u64, vp, vp, u64, i32, i32, vp]
         L.oracle_plan_bytes.restype = u64
         _LIB = L
     return _LIB
@@ -129,4 +131,21 @@ def time_scan_pair(plan: bytes, data: np.ndarray, iters: int = 1):
     d = np.ascontiguousarray(data, dtype=np.uint8)
     counts = np.zeros(3, np.uint64)
     s = L.oracle_time_scan_pair(p.ctypes.data, p.size, _ptr(d), d.size, iters, counts.ctypes.data)
+    return s, (int(counts[0]), int(counts[1]))
+
+
+def time_batch(plan: bytes, data: np.ndarray, offsets: np.ndarray, threads: int, iters: int = 1):
+    """Mean wall seconds per scan+pair pass over every document of a batch, the
+    documents spread over `threads` host threads, and (n_struct, n_brackets)."""
+    L = lib()
+    p = np.frombuffer(plan, np.uint8)
+    d = np.ascontiguousarray(data, dtype=np.uint8)
+    o = np.ascontiguousarray(offsets, dtype=np.uint64)
+    if o.size < 1 or int(o[-1]) > d.size:
+        raise ValueError("offsets exceed the data")
+    counts = np.zeros(2, np.uint64)
+    s = L.oracle_time_batch(p.ctypes.data, p.size, _ptr(d), o.ctypes.data, o.size - 1,
+                            threads, iters, counts.ctypes.data)
+    if s < 0:
+        raise ValueError("malformed scan_plan, offsets or thread count")
     return s, (int(counts[0]), int(counts[1]))

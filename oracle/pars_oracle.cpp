@@ -21,10 +21,12 @@
 //   4 ok 5 delim 6 escape [7,263) rep_of [263,327) trans[8][8] [327,391) masked[8][8]
 //   3176 n_descs
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -274,6 +276,73 @@ double oracle_time_scan_pair(
 		counts_out[0] = counts[0];
 		counts_out[1] = counts[1];
 		counts_out[2] = counts[2];
+	}
+	return std::chrono::duration<double>(t1 - t0).count() / iters;
+}
+
+// Runs scan then pair over every document of a batch (`offsets`: ndocs + 1 byte
+// offsets into `in`), `iters` times, spread over `threads` host threads that take
+// documents one at a time from a shared counter, and returns the mean wall seconds
+// per pass over the batch (the CPU baseline of the batched workload: the reference
+// scans a document sequentially, so a batch spreads documents over cores).
+// counts_out = {structurals, brackets} summed over the documents of one pass.
+double oracle_time_batch(
+	const std::uint8_t* plan, std::uint64_t plan_len, const std::uint8_t* in,
+	const std::uint64_t* offsets, std::uint64_t ndocs, int threads, int iters,
+	std::uint64_t* counts_out
+) {
+	Plan P;
+	if (!parse_plan(plan, plan_len, P) || iters <= 0 || threads <= 0 || !offsets)
+		return -1.0;
+	for (std::uint64_t d = 0; d < ndocs; ++d)
+		if (offsets[d + 1] < offsets[d])
+			return -1.0;
+	std::atomic<std::uint64_t> next {0}, n_struct {0}, n_brackets {0};
+	auto work = [&]() {
+		std::vector<std::uint32_t> pos, bpos;
+		std::vector<std::uint8_t>  chars, bchar;
+		std::vector<std::int32_t>  pair, depth;
+		std::uint64_t			   ns = 0, nb = 0;
+		for (;;) {
+			const std::uint64_t d = next.fetch_add(1, std::memory_order_relaxed);
+			if (d >= ndocs)
+				break;
+			const std::uint64_t n = offsets[d + 1] - offsets[d];
+			if (pos.size() < n) {
+				pos.resize(n);
+				bpos.resize(n);
+				chars.resize(n);
+				bchar.resize(n);
+				pair.resize(n);
+				depth.resize(n);
+			}
+			std::uint64_t counts[3] = {0, 0, 0};
+			std::int32_t  flags[3];
+			oracle_scan(
+				plan, plan_len, in + offsets[d], n, pos.data(), chars.data(), n, bpos.data(),
+				bchar.data(), n, nullptr, counts
+			);
+			oracle_pair(plan, plan_len, bchar.data(), counts[1], pair.data(), depth.data(), flags);
+			ns += counts[0];
+			nb += counts[1];
+		}
+		n_struct += ns;
+		n_brackets += nb;
+	};
+	const auto t0 = std::chrono::steady_clock::now();
+	for (int it = 0; it < iters; ++it) {
+		next	   = 0;
+		n_struct   = 0;
+		n_brackets = 0;
+		std::vector<std::thread> pool;
+		for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+		work();
+		for (auto& th : pool) th.join();
+	}
+	const auto t1 = std::chrono::steady_clock::now();
+	if (counts_out) {
+		counts_out[0] = n_struct;
+		counts_out[1] = n_brackets;
 	}
 	return std::chrono::duration<double>(t1 - t0).count() / iters;
 }
