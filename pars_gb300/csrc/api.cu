@@ -1210,6 +1210,8 @@ int pars_scan_host(pars_ctx* ctx, int plan_id, const uint8_t* h_in, uint64_t n, 
 	Plan* pl = get_plan(ctx, plan_id);
 	if (!pl || !out || (n && !h_in))
 		return ctx ? fail(ctx, PARS_EINVAL, "bad arguments") : PARS_EINVAL;
+	if (n >= (1ull << 32))	// before the document is staged on the device
+		return fail(ctx, PARS_ERANGE, "document larger than 2^32-1 bytes");
 	cudaSetDevice(ctx->device);
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	if (int r = grow(ctx, ctx->d_in, n + 16))
