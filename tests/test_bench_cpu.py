@@ -1,0 +1,48 @@
+"""bench.py's contract on the CPU: the reference arm prints one JSON line with the
+keys the measurement contract asks for, and the roofline's inputs (measured peak,
+per-launch DRAM traffic from the committed ncu summaries) resolve."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+LINE_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+             "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config")
+
+
+def test_reference_arm_prints_one_contract_line():
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
+                          "--warmup", "3"], capture_output=True, text=True, cwd=ROOT,
+                         timeout=600, check=True)
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in LINE_KEYS + ("impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["unit"] == "GB/s" and d["higher_is_better"]
+    assert d["config"]["workload"] == "csv_1GiB_single_document"
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+
+
+def test_roofline_inputs_resolve():
+    peak, kind = bench.peaks()
+    assert kind == "measured" and 1000 < peak < 20000
+    traffic = bench.traffic_from_profiles("k_scan_ws", "csv_1GiB_single_document")
+    assert traffic is not None and traffic > (1 << 30)  # at least the input, read once
+    assert bench.traffic_from_profiles("k_scan_ws", "no_such_workload") is None
+
+
+def test_reference_arm_on_other_ranks_prints_nothing():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2")
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
+                          "--warmup", "3"], capture_output=True, text=True, cwd=ROOT,
+                         timeout=600, check=True, env=env)
+    assert out.stdout.strip() == ""
