@@ -145,6 +145,10 @@ struct pars_server {
 	std::unordered_map<std::uint64_t, std::shared_ptr<Request>> all;
 	std::uint64_t					  next_ticket = 1;
 	bool							  stop		  = false;
+	// plan loads touch every worker's context: they wait until no launch is in
+	// flight (busy) and hold admissions back meanwhile (loading)
+	int								  busy		  = 0;
+	int								  loading	  = 0;
 	std::string						  err;
 	ResultPool						  pool;
 };
@@ -310,7 +314,7 @@ void worker_loop(pars_server* s, Worker* w) {
 		std::vector<std::shared_ptr<Request>> batch;
 		{
 			std::unique_lock<std::mutex> lk(s->mu);
-			s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+			s->cv_work.wait(lk, [&] { return s->stop || (!s->pending.empty() && !s->loading); });
 			if (s->stop)
 				return;
 			// admission: the oldest request's plan, then every pending request of that
@@ -340,6 +344,8 @@ void worker_loop(pars_server* s, Worker* w) {
 					++it;
 				}
 			}
+			if (!batch.empty())
+				++s->busy;
 		}
 		if (batch.empty())
 			continue;
@@ -353,6 +359,7 @@ void worker_loop(pars_server* s, Worker* w) {
 		{
 			std::lock_guard<std::mutex> lk(s->mu);
 			for (auto& r : batch) r->done_ns = t1;
+			--s->busy;
 		}
 		s->cv_done.notify_all();
 	}
@@ -447,16 +454,29 @@ int pars_server_destroy(pars_server* s) {
 int pars_server_plan_load(pars_server* s, const void* plan, size_t len, int* plan_id) {
 	if (!s || !plan || !plan_id)
 		return PARS_EINVAL;
-	std::lock_guard<std::mutex> lk(s->mu);
+	std::unique_lock<std::mutex> lk(s->mu);
+	// a context belongs to one thread at a time: load into the workers' contexts only
+	// while none of them runs a launch, and admit nothing until the load is done
+	++s->loading;
+	s->cv_done.wait(lk, [&] { return s->busy == 0; });
+	int rc = 0;
 	for (auto& w : s->workers) {
 		int id = -1;
-		if (int rc = pars_plan_load(w->ctx, plan, len, &id))
-			return rc;
+		if ((rc = pars_plan_load(w->ctx, plan, len, &id)) != 0)
+			break;
 		w->plan_ids.push_back(id);
 	}
-	s->plans.emplace_back(static_cast<const std::uint8_t*>(plan), static_cast<const std::uint8_t*>(plan) + len);
-	*plan_id = static_cast<int>(s->plans.size()) - 1;
-	return 0;
+	if (rc == 0) {
+		s->plans.emplace_back(static_cast<const std::uint8_t*>(plan), static_cast<const std::uint8_t*>(plan) + len);
+		*plan_id = static_cast<int>(s->plans.size()) - 1;
+	} else {
+		// every worker's table stays as long as the server's
+		for (auto& w : s->workers) w->plan_ids.resize(s->plans.size());
+	}
+	--s->loading;
+	lk.unlock();
+	s->cv_work.notify_all();
+	return rc;
 }
 
 int pars_server_submit(pars_server* s, int plan_id, const uint8_t* data, uint64_t n, uint32_t flags,

@@ -51,3 +51,30 @@ def test_server_results_equal_single_scans(max_batch_docs, result_mib):
         assert folded > 0, "no request shared a launch"
     else:
         assert folded == 0
+
+
+def test_plan_loads_while_requests_run():
+    """Plans loaded while earlier requests are queued and running: the loads wait for
+    the launches in flight, and every result still equals a single scan."""
+    srv = Server(arena_bytes=1 << 30, workers=2, max_batch_docs=4096)
+    plans = {"json": srv.load_plan(plan_bytes("json"))}
+    reqs = make_requests(23, 160)
+    tickets = []
+    for i, (g, t) in enumerate(reqs):
+        if g not in plans:
+            plans[g] = srv.load_plan(plan_bytes(g))  # requests of the first plan in flight
+        tickets.append(srv.submit(plans[g], t.data_ptr(), t.numel(), want_pairs=True))
+        if i == 80:
+            extra = srv.load_plan(plan_bytes("toml"))  # mid-stream, nothing of its plan queued
+    assert extra == len(plans)
+    got = [srv.wait(tk) for tk in tickets]
+    srv.close()
+    scanners = {g: Scanner(plan_bytes(g)) for g in ("json", "csv")}
+    for (g, t), r in zip(reqs, got):
+        assert r["status"] == 0
+        d = t.cuda()
+        e = scanners[g].scan_device(d.data_ptr(), d.numel(), want_pairs=True)
+        torch.cuda.synchronize()
+        en = e.to_numpy()
+        assert np.array_equal(r["pos"], en["pos"])
+        assert np.array_equal(r["pair"], en["pair"])
