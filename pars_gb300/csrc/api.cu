@@ -71,6 +71,7 @@ struct Plan {
 	DevPlan		   host;
 	DevPlan*	   dev = nullptr;
 	int			   path = kPathGeneric;
+	int			   helper_id = -1;	// this plan in the context's batch helper, once loaded
 };
 
 }  // namespace
@@ -1931,9 +1932,14 @@ extern "C" int pars_scan_batch(pars_ctx* ctx, int plan_id, const uint8_t* d_in, 
 		if (!B.helper)
 			if (int e = pars_create(ctx->device, 0, &B.helper))
 				return fail(ctx, e, "could not create the helper context");
-		int hp = -1;
-		if (int e = pars_plan_load(B.helper, &pl->raw, sizeof pl->raw, &hp))
-			return fail(ctx, e, "helper plan load failed");
+		// the helper keeps one copy of each plan across batch calls
+		if (pl->helper_id < 0) {
+			int id = -1;
+			if (int e = pars_plan_load(B.helper, &pl->raw, sizeof pl->raw, &id))
+				return fail(ctx, e, "helper plan load failed");
+			pl->helper_id = id;
+		}
+		const int hp = pl->helper_id;
 		uint64_t s_cur = region_s[G], b_cur = 0;
 		// per-document records of these documents, written after they are all scanned
 		struct Rec {

@@ -80,6 +80,8 @@ def test_batch_edge_documents(ctx):
     docs += lognormal_docs(7, 200, synth.json_doc, median=300, sigma=1.0)
     bv = check_batch(sc, docs)
     assert bv.n_recomputed >= 3
+    again = check_batch(sc, docs)  # the helper context keeps its copy of the plan
+    assert again.n_recomputed == bv.n_recomputed
 
 
 def test_batch_generic_plan(ctx):
