@@ -34,7 +34,11 @@ def test_reference_arm_prints_one_contract_line():
 
 def test_roofline_inputs_resolve():
     peak, kind = bench.peaks()
-    assert kind == "measured" and 1000 < peak < 20000
+    # the measured copy rate when the peaks file is present, else the stated fallback
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        assert kind == "measured" and 1000 < peak < 20000
+    else:
+        assert (kind, peak) == ("fallback", 6800.0)
     traffic = bench.traffic_from_profiles("k_scan_ws", "csv_1GiB_single_document")
     assert traffic is not None and traffic > (1 << 30)  # at least the input, read once
     assert bench.traffic_from_profiles("k_scan_ws", "no_such_workload") is None
