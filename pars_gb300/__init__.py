@@ -8,6 +8,8 @@ hand-written CUDA behind the C ABI of include/pars_gb300.h.
     sc = Scanner(open("json.plan", "rb").read())
     r = sc.scan_tensor(data_u8_cuda, want_pairs=True)
 """
-from .scanner import Context, DeviceResult, HostResult, Scanner  # noqa: F401
+from .scanner import (Context, DeviceResult, HostResult, Scanner, scan_chunk,  # noqa: F401
+                      scan_device, scan_host, thread_scanner)
 
-__all__ = ["Context", "Scanner", "DeviceResult", "HostResult"]
+__all__ = ["Context", "Scanner", "DeviceResult", "HostResult", "scan_device", "scan_host",
+           "scan_chunk", "thread_scanner"]

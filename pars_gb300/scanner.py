@@ -10,12 +10,18 @@
 * ``reserve_struct`` / ``scan_chunk`` / ``struct_ptr`` — chunked stage 1
   (pipeline.cuh:1214-1225), here for every plan kind with the carry kept on the device.
 
+The module-level ``scan_device`` / ``scan_host`` / ``scan_chunk`` correspond to the
+reference's free functions (pipeline.cuh:1260-1281), each of which keeps a
+``static thread_local scanner<S>``: here each (function, plan, device) has one
+Scanner, with its own context, per calling thread.
+
 Device results are borrowed from the context until its next scan, as in the
 reference; ``DeviceResult.*()`` return zero-copy torch views of those buffers.
 """
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -275,6 +281,50 @@ class Scanner:
         check(lib().pars_chunk_finish(self.ctx.handle, self.plan_id, ctypes.byref(carry), flags,
                                       ctypes.c_void_p(stream), ctypes.byref(r)), self.ctx.handle)
         return DeviceResult(r, int(carry.byte_base))
+
+
+_tls = threading.local()
+
+
+def thread_scanner(fn: str, plan: bytes, device: int = 0) -> Scanner:
+    """The calling thread's Scanner behind free function `fn` for `plan` on `device`
+    (cf. each free function's ``static thread_local scanner<S>``): created on first
+    use with a context of its own, so its borrowed results last until that function's
+    next call for the same plan on this thread."""
+    cache = getattr(_tls, "scanners", None)
+    if cache is None:
+        cache = _tls.scanners = {}
+    key = (fn, bytes(plan), device)
+    sc = cache.get(key)
+    if sc is None:
+        sc = cache[key] = Scanner(plan, device=device)
+    return sc
+
+
+def scan_device(plan: bytes, d_ptr: int, n: int, stream: int = 0, want_pairs: bool = False,
+                device: int = 0) -> DeviceResult:
+    """Free ``scan_device<S>(d_data, n, s, want_pairs)`` (pipeline.cuh:1260-1266)."""
+    return thread_scanner("scan_device", plan, device).scan_device(
+        d_ptr, n, stream=stream, want_pairs=want_pairs)
+
+
+def scan_host(plan: bytes, data, want_pairs: bool = False, device: int = 0) -> HostResult:
+    """Free ``scan_host<S>(h_data, n, want_pairs)`` (pipeline.cuh:1268-1272)."""
+    return thread_scanner("scan_host", plan, device).scan_host(data, want_pairs=want_pairs)
+
+
+def scan_chunk(plan: bytes, d_chunk: int, n: int, carry: _lib.ChunkCarry | None = None,
+               stream: int = 0, device: int = 0) -> _lib.ChunkCarry:
+    """Free ``scan_chunk<S>(d_chunk, n, in, s, byte_base)`` (pipeline.cuh:1274-1281):
+    scans the next chunk of a document and returns the carry for the one after it.
+    Start a document with ``carry=None``; the carry tracks the byte base itself, so
+    there is no byte_base argument.  The offsets accumulate in the thread's
+    scan_chunk Scanner: ``thread_scanner("scan_chunk", plan).chunk_finish(carry)``
+    closes the document."""
+    sc = thread_scanner("scan_chunk", plan, device)
+    c = carry if carry is not None else sc.new_carry()
+    sc.scan_chunk(d_chunk, n, c, stream)
+    return c
 
 
 class BatchView:

@@ -392,3 +392,27 @@ def test_nesting_beyond_one_digit(scanners, depth, tail):
     data = np.frombuffer(b"[" * depth + b"1" + b"]" * depth + tail, np.uint8).copy()
     e = expected_from_oracle(plan, data)
     compare(run(scanners["json"], data), e, f"depth {depth} + {tail!r}")
+
+
+def test_free_functions():
+    """The free functions (cf. pipeline.cuh:1260-1281) scan like a Scanner, and a
+    result stays valid while the same thread scans another plan."""
+    import pars_gb300
+    pj, pc = plan_bytes("json"), plan_bytes("csv")
+    dj, dc = synth.json_doc(31, 1 << 20), synth.csv_doc(32, 1 << 20)
+    tj, tc = torch.from_numpy(dj).cuda(), torch.from_numpy(dc).cuda()
+    rj = pars_gb300.scan_device(pj, tj.data_ptr(), tj.numel(), want_pairs=True)
+    rc = pars_gb300.scan_device(pc, tc.data_ptr(), tc.numel())
+    torch.cuda.synchronize()
+    ej, ec = oracle.scan(pj, dj), oracle.scan(pc, dc)
+    assert np.array_equal(rj.to_numpy()["pos"], ej.positions)
+    assert np.array_equal(rc.to_numpy()["pos"], ec.positions)
+    hr = pars_gb300.scan_host(pj, dj, want_pairs=True)
+    assert np.array_equal(hr.structural, ej.positions)
+    pars_gb300.thread_scanner("scan_chunk", pc).reserve_struct(dc.size + 1024)
+    carry = None
+    for off in range(0, dc.size, 300_000):
+        carry = pars_gb300.scan_chunk(pc, tc.data_ptr() + off, min(300_000, dc.size - off), carry)
+    r = pars_gb300.thread_scanner("scan_chunk", pc).chunk_finish(carry)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.to_numpy()["pos"], ec.positions)
