@@ -89,3 +89,24 @@ def test_struct_layouts_match_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(st), cname
         for field, _ in st._fields_:
             assert got[(cname, field)] == getattr(st, field).offset, (cname, field)
+
+
+def test_plan_shapes_match_the_reference_static_asserts():
+    """The committed plan bytes satisfy the reference's compile-time checks of the
+    plans it lowers (tests/test_model.cpp:29-75): bracket, mode, punctuation and
+    comment counts, the JSON / CSV mode bytes and the descriptor kinds
+    (lex_kind: affine 0, comment 1, doubled 2, table 3; include/pars/plan.hpp:54)."""
+    def shape(g):
+        b = plan_bytes(g)
+        nd = b[3176]
+        return {"n_punct": b[44], "n_brackets": b[45], "n_modes": b[46], "n_comments": b[47],
+                "mode0": (chr(b[24]), chr(b[25])),
+                "kinds": [b[48 + 391 * d] for d in range(nd)]}
+    j, c, t, k = shape("json"), shape("csv"), shape("toml"), shape("clike")
+    assert (j["n_brackets"], j["n_modes"], j["n_punct"]) == (2, 1, 2)
+    assert j["mode0"] == ('"', "\\") and j["kinds"].count(0) == 1
+    assert (c["n_brackets"], c["n_modes"], c["n_punct"]) == (0, 1, 2)
+    assert c["mode0"] == ('"', '"') and c["kinds"].count(2) == 1
+    assert (t["n_brackets"], t["n_modes"], t["n_comments"], t["n_punct"]) == (2, 2, 1, 3)
+    assert t["kinds"].count(1) == 1
+    assert (k["n_brackets"], k["n_punct"]) == (1, 1) and 3 in k["kinds"]
