@@ -110,3 +110,16 @@ def test_plan_shapes_match_the_reference_static_asserts():
     assert (t["n_brackets"], t["n_modes"], t["n_comments"], t["n_punct"]) == (2, 2, 1, 3)
     assert t["kinds"].count(1) == 1
     assert (k["n_brackets"], k["n_punct"]) == (1, 1) and 3 in k["kinds"]
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No fallback: without libpars_gb300.so every entry point raises instead of
+    computing anything on the CPU."""
+    from pars_gb300 import _lib
+    from pars_gb300 import scanner as S
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libpars_gb300.so"))
+    monkeypatch.setattr(_lib, "_LIB", None)
+    with pytest.raises(ImportError):
+        _lib.lib()
+    with pytest.raises(ImportError):
+        S.Context(0)
